@@ -1,0 +1,29 @@
+// em_kernels.cuh -- launchers shared between the EM translation units.
+#pragma once
+
+#include "fem_internal.cuh"
+
+namespace fem {
+
+// em_plain.cu
+int em_plain_estep(fem_em *h);
+int em_plain_mstep(fem_em *h);
+int em_factor(fem_em *h, bool regularize);
+int64_t em_plain_logl_blocks(int64_t n, int d);
+void cov_geometry(int d, int *TB, int *nb, int *nblk);
+int em_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);
+int em_classes(fem_em *h, int32_t *dcls);
+
+// em_tc.cu (tcgen05 mixed precision)
+bool em_tc_supported(int d, int k);
+int em_tc_create(fem_em *h);
+void em_tc_destroy(fem_em *h);
+int em_tc_upload(fem_em *h);    // X -> bf16 hi/lo split
+int em_tc_prepare(fem_em *h);   // factors -> permuted bf16 hi/lo operands + offsets
+int em_tc_estep(fem_em *h);
+int em_tc_mstep(fem_em *h);
+
+// host_linalg.cpp
+double host_cond_number(int d, const double *sigma);
+
+}  // namespace fem

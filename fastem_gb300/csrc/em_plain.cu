@@ -1,0 +1,672 @@
+// em_plain.cu -- CUDA-core EM sweep in FP32 or FP64 (the "plain" precision
+// forms), plus the FP64 per-component factorisation shared by every form.
+//
+// One sweep = SimpleMatrixEM::PrecomputeDensityMatrix + MStep + the
+// RegularizeCovariances / InitDensities that TrainNoCopy runs after it
+// (EM2/MatrixEM.cpp:275-378, EM2/EMAlgorithm.cpp:139-191).
+//
+// Layout in HBM: X is n x d float rows; posteriors R are component-major
+// (k x n) so every per-component pass streams contiguous memory; the
+// inverse Cholesky factors are stored as W_j = L_j^-1 (lower, row-major), so
+// the Mahalanobis term of point x is ||W_j (x - mu_j)||^2 (the reference
+// multiplies by CholInvC = W_j^T from the right, EM2/MatrixEM.cpp:76).
+#include <cfloat>
+#include <cmath>
+
+#include "fem_internal.cuh"
+#include "em_kernels.cuh"
+
+namespace fem {
+
+// ------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// deterministic block sum (fixed shuffle tree, fixed warp order); result in thread 0
+template <int NT>
+__device__ double block_sum(double v, double *red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; i++) s += red[i];
+  return s;
+}
+
+template <typename T> __device__ __forceinline__ T t_exp(T x);
+template <> __device__ __forceinline__ float t_exp(float x) { return expf(x); }
+template <> __device__ __forceinline__ double t_exp(double x) { return exp(x); }
+template <typename T> __device__ __forceinline__ T t_log(T x);
+template <> __device__ __forceinline__ float t_log(float x) { return logf(x); }
+template <> __device__ __forceinline__ double t_log(double x) { return log(x); }
+
+// online log-sum-exp step (max-shifted), -inf entries contribute nothing
+template <typename T>
+__device__ __forceinline__ void lse_push(T l, T &mx, T &se) {
+  if (l > mx) {
+    se = se * t_exp(mx - l) + T(1);
+    mx = l;
+  } else if (l > -INFINITY) {
+    se += t_exp(l - mx);
+  }
+}
+
+// ================================================================ E-step
+// MatrixEMBase::BlockDensities + PostProcessDensityMatrix
+// (EM2/MatrixEM.cpp:39-51,69-81): one thread per point, components staged
+// through shared memory; l_ij is written to R, then overwritten by
+// exp(l_ij - LSE_i).  D > 0: compile-time dimension with the centred point
+// in registers.
+template <typename T, int D>
+__global__ void __launch_bounds__(128)
+k_estep_plain(const float *__restrict__ X, int64_t n, int K, const T *__restrict__ mu,
+              const T *__restrict__ W, const T *__restrict__ logc, T *__restrict__ R,
+              double *__restrict__ part) {
+  __shared__ __align__(16) T sW[D * D];
+  __shared__ __align__(16) T smu[D];
+  __shared__ double red[4];
+  const int tid = threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * 128 + tid;
+  const bool valid = i < n;
+  float x[D];
+#pragma unroll
+  for (int q = 0; q < D; q++) x[q] = valid ? X[i * D + q] : 0.f;
+  T mx = -INFINITY, se = T(0);
+  for (int j = 0; j < K; j++) {
+    __syncthreads();
+    for (int e = tid; e < D * D; e += 128) sW[e] = W[(size_t)j * D * D + e];
+    if (tid < D) smu[tid] = mu[(size_t)j * D + tid];
+    __syncthreads();
+    T t[D];
+#pragma unroll
+    for (int q = 0; q < D; q++) t[q] = (T)x[q] - smu[q];
+    T s = T(0);
+#pragma unroll
+    for (int kk = 0; kk < D; kk++) {
+      T y = T(0);
+#pragma unroll
+      for (int m = 0; m <= kk; m++) y = fma(t[m], sW[kk * D + m], y);
+      s = fma(y, y, s);
+    }
+    const T l = logc[j] - T(0.5) * s;
+    if (valid) R[(size_t)j * n + i] = l;
+    lse_push(l, mx, se);
+  }
+  const T lse = mx + t_log(se);
+  if (valid)
+    for (int j = 0; j < K; j++) {
+      T *p = R + (size_t)j * n + i;
+      *p = t_exp(*p - lse);
+    }
+  double s = block_sum<128>(valid ? (double)lse : 0.0, red);
+  if (tid == 0) part[blockIdx.x] = s;
+}
+
+// runtime dimension: centred point in shared memory, factor read through L1
+template <typename T>
+__global__ void __launch_bounds__(64)
+k_estep_plain_generic(const float *__restrict__ X, int64_t n, int d, int K,
+                      const T *__restrict__ mu, const T *__restrict__ W,
+                      const T *__restrict__ logc, T *__restrict__ R, double *__restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sT = (T *)smem_raw;  // 64 x (d+1)
+  __shared__ double red[2];
+  const int tid = threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * 64 + tid;
+  const bool valid = i < n;
+  T *t = sT + (size_t)tid * (d + 1);
+  T mx = -INFINITY, se = T(0);
+  for (int j = 0; j < K; j++) {
+    const T *mj = mu + (size_t)j * d;
+    const T *Wj = W + (size_t)j * d * d;
+    for (int q = 0; q < d; q++) t[q] = valid ? ((T)X[i * d + q] - mj[q]) : T(0);
+    T s = T(0);
+    for (int kk = 0; kk < d; kk++) {
+      const T *wr = Wj + (size_t)kk * d;
+      T y = T(0);
+      for (int m = 0; m <= kk; m++) y = fma(t[m], wr[m], y);
+      s = fma(y, y, s);
+    }
+    const T l = logc[j] - T(0.5) * s;
+    if (valid) R[(size_t)j * n + i] = l;
+    lse_push(l, mx, se);
+  }
+  const T lse = mx + t_log(se);
+  if (valid)
+    for (int j = 0; j < K; j++) {
+      T *p = R + (size_t)j * n + i;
+      *p = t_exp(*p - lse);
+    }
+  double s = block_sum<64>(valid ? (double)lse : 0.0, red);
+  if (tid == 0) part[blockIdx.x] = s;
+}
+
+// single-block deterministic sum of the per-block log-likelihood partials
+__global__ void __launch_bounds__(1024) k_reduce_logl(const double *part, int64_t np, DevStatus *st) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int64_t b = threadIdx.x; b < np; b += 1024) v += part[b];
+  double s = block_sum<1024>(v, red);
+  if (threadIdx.x == 0) st->logl = s;
+}
+
+// ======================================================= M-step: means
+// SimpleMatrixEM::doMStep means part (EM2/MatrixEM.cpp:319-343):
+// PosteriorSum_j = sum_i r_ij and MeanSums_j = sum_i r_ij x_i per block of
+// rows; each thread owns (component, C-column chunk) units.
+constexpr int kMeanTP = 32;
+
+template <typename T, int C, int UPT>
+__global__ void __launch_bounds__(256)
+k_means_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__restrict__ R,
+              double *__restrict__ part, int64_t rows_per_block) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *sX = (float *)smem_raw;                       // TP x d
+  T *sR = (T *)(sX + kMeanTP * d);                     // K x (TP+1)
+  const int tid = threadIdx.x;
+  const int nch = d / C, units = K * nch;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = min(n, r0 + rows_per_block);
+  T acc[UPT][C], acc1[UPT];
+  double dacc[UPT][C], dacc1[UPT];
+#pragma unroll
+  for (int u = 0; u < UPT; u++) {
+    acc1[u] = T(0);
+    dacc1[u] = 0.0;
+#pragma unroll
+    for (int a = 0; a < C; a++) acc[u][a] = T(0), dacc[u][a] = 0.0;
+  }
+  int tiles = 0;
+  for (int64_t t0 = r0; t0 < r1; t0 += kMeanTP) {
+    const int tp = (int)min((int64_t)kMeanTP, r1 - t0);
+    __syncthreads();
+    for (int e = tid; e < kMeanTP * d; e += 256) {
+      int p = e / d;
+      sX[e] = (p < tp) ? X[(t0 + p) * d + (e - p * d)] : 0.f;
+    }
+    for (int e = tid; e < K * kMeanTP; e += 256) {
+      int j = e / kMeanTP, p = e - j * kMeanTP;
+      sR[j * (kMeanTP + 1) + p] = (p < tp) ? R[(size_t)j * n + t0 + p] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < UPT; u++) {
+      const int unit = tid + u * 256;
+      if (unit < units) {
+        const int j = unit / nch, c = unit - j * nch;
+        const T *rr = sR + j * (kMeanTP + 1);
+        const float *xx = sX + c * C;
+        for (int p = 0; p < kMeanTP; p++) {
+          const T r = rr[p];
+          acc1[u] += r;
+#pragma unroll
+          for (int a = 0; a < C; a++) acc[u][a] = fma(r, (T)xx[p * d + a], acc[u][a]);
+        }
+      }
+    }
+    // flush the short-range accumulators into FP64 every 16 tiles
+    if (++tiles == 16 || t0 + kMeanTP >= r1) {
+      tiles = 0;
+#pragma unroll
+      for (int u = 0; u < UPT; u++) {
+        dacc1[u] += (double)acc1[u];
+        acc1[u] = T(0);
+#pragma unroll
+        for (int a = 0; a < C; a++) {
+          dacc[u][a] += (double)acc[u][a];
+          acc[u][a] = T(0);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < UPT; u++) {
+    const int unit = tid + u * 256;
+    if (unit < units) {
+      const int j = unit / nch, c = unit - j * nch;
+      double *o = part + ((size_t)blockIdx.x * K + j) * (d + 1);
+      if (c == 0) o[0] = dacc1[u];
+#pragma unroll
+      for (int a = 0; a < C; a++) o[1 + c * C + a] = dacc[u][a];
+    }
+  }
+}
+
+// PosteriorSum, Means = MeanSums / PosteriorSum, Probs = PosteriorSum / N
+// (EM2/MatrixEM.cpp:341-343,375); one block per component, blocks summed in order
+template <typename T>
+__global__ void k_final_means(const double *__restrict__ part, int G, int K, int d, int64_t n,
+                              double *__restrict__ mu, double *__restrict__ pi,
+                              double *__restrict__ psum, T *__restrict__ muT) {
+  const int j = blockIdx.x;
+  __shared__ double s1;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += part[((size_t)g * K + j) * (d + 1)];
+    s1 = s;
+    psum[j] = s;
+    pi[j] = s / (double)n;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < d; q += blockDim.x) {
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += part[((size_t)g * K + j) * (d + 1) + 1 + q];
+    const double m = s / s1;
+    mu[(size_t)j * d + q] = m;
+    muT[(size_t)j * d + q] = (T)m;
+  }
+}
+
+// ================================================== M-step: covariances
+// MatrixEMBase::ComputeWeightedTempDataset + BlockCovariances
+// (EM2/MatrixEM.cpp:53-67,90-99): z = sqrt(r_ij) (x_i - mu_j), CovSum_j +=
+// z z^T over the upper block triangle.  Each thread owns one TB x TB block
+// of one component; a CTA owns 256 consecutive (component, block) units.
+constexpr int kCovTP = 32;
+
+template <typename T, int TB>
+__global__ void __launch_bounds__(256)
+k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__restrict__ R,
+            const T *__restrict__ mu, double *__restrict__ part, int nb, int nblk,
+            int64_t rows_per_chunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sZ = (T *)smem_raw;  // CJ x TP x d
+  const int tid = threadIdx.x;
+  const int u0 = blockIdx.x * 256;
+  const int j_lo = u0 / nblk;
+  const int j_hi = min(K - 1, (u0 + 255) / nblk);
+  const int CJ = j_hi - j_lo + 1;
+  const int unit = u0 + tid;
+  const bool valid = unit < K * nblk;
+  int j = 0, bi = 0, bj = 0;
+  if (valid) {
+    j = unit / nblk;
+    int b = unit - j * nblk;
+    // upper-triangular enumeration of nb x nb blocks: row bi has nb - bi blocks
+    while (b >= nb - bi) {
+      b -= nb - bi;
+      bi++;
+    }
+    bj = bi + b;
+  }
+  const int64_t c0 = (int64_t)blockIdx.y * rows_per_chunk;
+  const int64_t c1 = min(n, c0 + rows_per_chunk);
+  T acc[TB][TB];
+#pragma unroll
+  for (int a = 0; a < TB; a++)
+#pragma unroll
+    for (int b = 0; b < TB; b++) acc[a][b] = T(0);
+  const int cj = j - j_lo;
+  for (int64_t t0 = c0; t0 < c1; t0 += kCovTP) {
+    const int tp = (int)min((int64_t)kCovTP, c1 - t0);
+    __syncthreads();
+    const int tot = CJ * kCovTP * d;
+    for (int e = tid; e < tot; e += 256) {
+      const int jj = e / (kCovTP * d);
+      const int rem = e - jj * kCovTP * d;
+      const int p = rem / d, a = rem - p * d;
+      T z = T(0);
+      if (p < tp) {
+        const int64_t row = t0 + p;
+        const T r = R[(size_t)(j_lo + jj) * n + row];
+        z = sqrt(r) * ((T)X[row * d + a] - mu[(size_t)(j_lo + jj) * d + a]);
+      }
+      sZ[e] = z;
+    }
+    __syncthreads();
+    if (valid) {
+      const T *zb = sZ + (size_t)cj * kCovTP * d;
+      for (int p = 0; p < kCovTP; p++) {
+        const T *zr = zb + p * d;
+        T va[TB], vb[TB];
+#pragma unroll
+        for (int a = 0; a < TB; a++) va[a] = zr[bi * TB + a];
+#pragma unroll
+        for (int b = 0; b < TB; b++) vb[b] = zr[bj * TB + b];
+#pragma unroll
+        for (int a = 0; a < TB; a++)
+#pragma unroll
+          for (int b = 0; b < TB; b++) acc[a][b] = fma(va[a], vb[b], acc[a][b]);
+      }
+    }
+  }
+  if (valid) {
+    double *o = part + (((size_t)blockIdx.y * K + j) * nblk + (unit - j * nblk)) * (TB * TB);
+#pragma unroll
+    for (int a = 0; a < TB; a++)
+#pragma unroll
+      for (int b = 0; b < TB; b++) o[a * TB + b] = (double)acc[a][b];
+  }
+}
+
+// Covs_j = CovSum_j / PosteriorSum_j, upper mirrored to lower (EM2/MatrixEM.cpp:370-373)
+__global__ void k_final_cov(const double *__restrict__ part, int chunks, int K, int d, int nb,
+                            int nblk, int TB, const double *__restrict__ psum,
+                            double *__restrict__ sigma) {
+  const int j = blockIdx.x;
+  const double inv = 1.0 / psum[j];
+  double *S = sigma + (size_t)j * d * d;
+  const int per = TB * TB;
+  for (int e = threadIdx.x; e < nblk * per; e += blockDim.x) {
+    int b = e / per, w = e - b * per;
+    int bi = 0, bb = b;
+    while (bb >= nb - bi) {
+      bb -= nb - bi;
+      bi++;
+    }
+    const int bj = bi + bb;
+    const int a = bi * TB + w / TB, c = bj * TB + (w % TB);
+    if (a > c) continue;  // lower half of a diagonal block
+    double s = 0.0;
+    for (int ch = 0; ch < chunks; ch++) s += part[(((size_t)ch * K + j) * nblk + b) * per + w];
+    s *= inv;
+    S[(size_t)a * d + c] = s;
+    S[(size_t)c * d + a] = s;
+  }
+}
+
+// ======================================================= factorisation
+// EMAlgorithm::RegularizeCovariances + NormalDensity::Init + CalcLogCoeffs
+// (EM2/EMAlgorithm.cpp:237-244, EM2/NormalDensity.cpp:43-65,
+// EM2/MatrixEM.cpp:83-87) in FP64, one CTA per component: symmetric copy of
+// the lower triangle, right-looking Cholesky (a pivot <= 0 fails, as in
+// Eigen's LLT), log det = 2 sum log L_ii, W = L^-1 by column substitution,
+// log coefficient log pi_j - d/2 log 2pi - 1/2 log det.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_factor(int K, int d, double reg, int regularize, double *__restrict__ sigma,
+         const double *__restrict__ pi, const double *__restrict__ mu, double *__restrict__ work,
+         double *__restrict__ linv, double *__restrict__ logdet, double *__restrict__ logc,
+         T *__restrict__ muT, T *__restrict__ linvT, T *__restrict__ logcT, DevStatus *st) {
+  const int j = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  double *S = sigma + (size_t)j * d * d;
+  double *A = work + (size_t)j * d * d;
+  double *Wi = linv + (size_t)j * d * d;
+  __shared__ double s_piv;
+  __shared__ int s_fail;
+  if (regularize && reg != 0.0) {
+    if (tid == 0) {
+      double tr = 0.0;
+      for (int q = 0; q < d; q++) tr += S[(size_t)q * d + q];
+      s_piv = reg * tr / (double)d;
+    }
+    __syncthreads();
+    const double add = s_piv;
+    for (int e = tid; e < d * d; e += nt) {
+      const int r = e / d, c = e - r * d;
+      S[e] = S[e] * (1.0 - reg) + (r == c ? add : 0.0);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < d * d; e += nt) {
+    const int r = e / d, c = e - r * d;
+    A[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
+  }
+  if (tid == 0) s_fail = 0;
+  __syncthreads();
+  for (int k = 0; k < d; k++) {
+    if (tid == 0) {
+      const double x = A[(size_t)k * d + k];
+      if (!(x > 0.0)) {
+        s_fail = 1;
+      } else {
+        const double l = sqrt(x);
+        A[(size_t)k * d + k] = l;
+        s_piv = l;
+      }
+    }
+    __syncthreads();
+    if (s_fail) break;
+    const double lkk = s_piv;
+    for (int i = k + 1 + tid; i < d; i += nt) A[(size_t)i * d + k] /= lkk;
+    __syncthreads();
+    // trailing update of the lower triangle: A[i][c] -= L[i][k] L[c][k], k < c <= i
+    const int m = d - k - 1;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = e / m, c = e - i * m;
+      if (c > i) continue;
+      const int gi = k + 1 + i, gc = k + 1 + c;
+      A[(size_t)gi * d + gc] -= A[(size_t)gi * d + k] * A[(size_t)gc * d + k];
+    }
+    __syncthreads();
+  }
+  if (s_fail) {
+    if (tid == 0) atomicMin(&st->chol_failed, j);
+    return;
+  }
+  // W = L^-1, column c by forward substitution (threads own columns)
+  for (int c = tid; c < d; c += nt) {
+    for (int r = 0; r < c; r++) Wi[(size_t)r * d + c] = 0.0;
+    for (int r = c; r < d; r++) {
+      double s = (r == c) ? 1.0 : 0.0;
+      for (int m2 = c; m2 < r; m2++) s -= A[(size_t)r * d + m2] * Wi[(size_t)m2 * d + c];
+      Wi[(size_t)r * d + c] = s / A[(size_t)r * d + r];
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double ld = 0.0;
+    for (int q = 0; q < d; q++) ld += log(A[(size_t)q * d + q]);
+    ld *= 2.0;
+    logdet[j] = ld;
+    const double lc = log(pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
+    logc[j] = lc;
+    logcT[j] = (T)lc;
+  }
+  for (int e = tid; e < d * d; e += nt) linvT[(size_t)j * d * d + e] = (T)Wi[e];
+  for (int q = tid; q < d; q += nt) muT[(size_t)j * d + q] = (T)mu[(size_t)j * d + q];
+}
+
+// =========================================================== launchers
+template <typename T>
+static int estep_plain_t(fem_em *h) {
+  const int64_t n = h->n;
+  const int d = h->d, K = h->k;
+  const T *mu = (const T *)h->muT, *W = (const T *)h->linvT, *lc = (const T *)h->logcT;
+  T *R = (T *)h->R;
+  cudaStream_t s = h->stream;
+  int64_t nb;
+#define FEM_EPL(DD)                                                                        \
+  case DD:                                                                                 \
+    nb = (n + 127) / 128;                                                                  \
+    k_estep_plain<T, DD><<<(unsigned)nb, 128, 0, s>>>(h->X, n, K, mu, W, lc, R, h->logl_part); \
+    break;
+  switch (d) {
+    FEM_EPL(4)
+    FEM_EPL(8)
+    FEM_EPL(16)
+    FEM_EPL(32)
+    FEM_EPL(64)
+    default: {
+      nb = (n + 63) / 64;
+      size_t sm = (size_t)64 * (d + 1) * sizeof(T);
+      if (sm > 48 * 1024)
+        FEM_CUDA(cudaFuncSetAttribute(k_estep_plain_generic<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      k_estep_plain_generic<T><<<(unsigned)nb, 64, sm, s>>>(h->X, n, d, K, mu, W, lc, R,
+                                                            h->logl_part);
+    }
+  }
+#undef FEM_EPL
+  FEM_CUDA(cudaGetLastError());
+  k_reduce_logl<<<1, 1024, 0, s>>>(h->logl_part, nb, h->dstat);
+  FEM_CUDA(cudaGetLastError());
+  h->launches += 2;
+  return FEM_OK;
+}
+
+int em_plain_estep(fem_em *h) {
+  return h->cfg.precision == FEM_PREC_FP64 ? estep_plain_t<double>(h) : estep_plain_t<float>(h);
+}
+
+int64_t em_plain_logl_blocks(int64_t n, int d) {
+  switch (d) {
+    case 4: case 8: case 16: case 32: case 64: return (n + 127) / 128;
+    default: return (n + 63) / 64;
+  }
+}
+
+void cov_geometry(int d, int *TB, int *nb, int *nblk) {
+  *TB = d >= 8 ? 8 : d;
+  *nb = (d + *TB - 1) / *TB;
+  *nblk = (*nb) * (*nb + 1) / 2;
+}
+
+template <typename T, int C>
+static int launch_means(fem_em *h, int upt, int64_t rpb, size_t sm) {
+  const T *R = (const T *)h->R;
+#define FEM_ML(U)                                                                          \
+  if (upt == U) {                                                                          \
+    if (sm > 48 * 1024)                                                                    \
+      FEM_CUDA(cudaFuncSetAttribute(k_means_plain<T, C, U>,                                \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    k_means_plain<T, C, U><<<h->mgrid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, R,     \
+                                                             h->mpart, rpb);               \
+    return FEM_OK;                                                                         \
+  }
+  FEM_ML(1)
+  FEM_ML(2)
+  FEM_ML(4)
+#undef FEM_ML
+  set_error("means kernel: %d units per thread unsupported", upt);
+  return FEM_ERR_UNSUPPORTED;
+}
+
+template <typename T, int TB>
+static int launch_cov(fem_em *h, int nb, int nblk, int64_t rpc) {
+  const int units = h->k * nblk;
+  const int gx = (units + 255) / 256;
+  const int cjmax = 256 / nblk + 2;
+  size_t sm = (size_t)min(cjmax, h->k) * kCovTP * h->d * sizeof(T);
+  if (sm > 48 * 1024)
+    FEM_CUDA(cudaFuncSetAttribute(k_cov_plain<T, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sm));
+  dim3 grid(gx, h->cchunks);
+  k_cov_plain<T, TB><<<grid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, (const T *)h->R,
+                                                   (const T *)h->muT, h->cpart, nb, nblk, rpc);
+  return FEM_OK;
+}
+
+template <typename T>
+static int mstep_plain_t(fem_em *h) {
+  const int d = h->d, K = h->k;
+  const int64_t n = h->n;
+  const int C = d < 32 ? d : 32;
+  const int units = K * (d / C);
+  const int upt = units <= 256 ? 1 : (units <= 512 ? 2 : (units <= 1024 ? 4 : 0));
+  if (upt == 0 || d % C) {
+    set_error("plain M-step: k*d too large (k=%d d=%d)", K, d);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  const int64_t rpb = (n + h->mgrid - 1) / h->mgrid;
+  size_t sm = (size_t)kMeanTP * d * sizeof(float) + (size_t)K * (kMeanTP + 1) * sizeof(T);
+  int st;
+  switch (C) {
+    case 4: st = launch_means<T, 4>(h, upt, rpb, sm); break;
+    case 8: st = launch_means<T, 8>(h, upt, rpb, sm); break;
+    case 16: st = launch_means<T, 16>(h, upt, rpb, sm); break;
+    case 32: st = launch_means<T, 32>(h, upt, rpb, sm); break;
+    default: set_error("unsupported d=%d", d); return FEM_ERR_UNSUPPORTED;
+  }
+  FEM_TRY(st);
+  FEM_CUDA(cudaGetLastError());
+  k_final_means<T><<<K, 128, 0, h->stream>>>(h->mpart, h->mgrid, K, d, n, h->mu, h->pi, h->psum,
+                                             (T *)h->muT);
+  FEM_CUDA(cudaGetLastError());
+  int TB, nb, nblk;
+  cov_geometry(d, &TB, &nb, &nblk);
+  const int64_t rpc = (n + h->cchunks - 1) / h->cchunks;
+  if (TB == 8)
+    st = launch_cov<T, 8>(h, nb, nblk, rpc);
+  else if (TB == 4)
+    st = launch_cov<T, 4>(h, nb, nblk, rpc);
+  else if (TB == 2)
+    st = launch_cov<T, 2>(h, nb, nblk, rpc);
+  else
+    st = launch_cov<T, 1>(h, nb, nblk, rpc);
+  FEM_TRY(st);
+  FEM_CUDA(cudaGetLastError());
+  k_final_cov<<<K, 256, 0, h->stream>>>(h->cpart, h->cchunks, K, d, nb, nblk, TB, h->psum,
+                                        h->sigma);
+  FEM_CUDA(cudaGetLastError());
+  h->launches += 4;
+  return FEM_OK;
+}
+
+int em_plain_mstep(fem_em *h) {
+  return h->cfg.precision == FEM_PREC_FP64 ? mstep_plain_t<double>(h) : mstep_plain_t<float>(h);
+}
+
+int em_factor(fem_em *h, bool regularize) {
+  const int K = h->k, d = h->d;
+  if (h->cfg.precision == FEM_PREC_FP64)
+    k_factor<double><<<K, 256, 0, h->stream>>>(K, d, h->cfg.reg_coef, regularize, h->sigma, h->pi,
+                                               h->mu, h->work, h->linv, h->logdet, h->logc,
+                                               (double *)h->muT, (double *)h->linvT,
+                                               (double *)h->logcT, h->dstat);
+  else
+    k_factor<float><<<K, 256, 0, h->stream>>>(K, d, h->cfg.reg_coef, regularize, h->sigma, h->pi,
+                                              h->mu, h->work, h->linv, h->logdet, h->logc,
+                                              (float *)h->muT, (float *)h->linvT,
+                                              (float *)h->logcT, h->dstat);
+  FEM_CUDA(cudaGetLastError());
+  h->launches += 1;
+  return FEM_OK;
+}
+
+// ------------------------------------------------ posteriors read-back
+template <typename T>
+__global__ void k_post_rows(const T *__restrict__ R, int64_t n, int K, int64_t r0, int64_t rows,
+                            double *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * K) return;
+  const int64_t i = e / K;
+  const int j = (int)(e - i * K);
+  out[e] = (double)R[(size_t)j * n + r0 + i];
+}
+
+// EMAlgorithm::RetrieveClasses: first index of the largest posterior
+template <typename T>
+__global__ void k_classes(const T *__restrict__ R, int64_t n, int K, int32_t *__restrict__ cls) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double best = -1.0;
+  int bj = -1;
+  for (int j = 0; j < K; j++) {
+    const double v = (double)R[(size_t)j * n + i];
+    if (v > best) {
+      best = v;
+      bj = j;
+    }
+  }
+  cls[i] = bj;
+}
+
+int em_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout) {
+  const int64_t tot = rows * h->k;
+  const unsigned nb = (unsigned)((tot + 255) / 256);
+  if (h->cfg.precision == FEM_PREC_FP64)
+    k_post_rows<double><<<nb, 256, 0, h->stream>>>((const double *)h->R, h->n, h->k, r0, rows, dout);
+  else
+    k_post_rows<float><<<nb, 256, 0, h->stream>>>((const float *)h->R, h->n, h->k, r0, rows, dout);
+  FEM_CUDA(cudaGetLastError());
+  return FEM_OK;
+}
+
+int em_classes(fem_em *h, int32_t *dcls) {
+  const unsigned nb = (unsigned)((h->n + 255) / 256);
+  if (h->cfg.precision == FEM_PREC_FP64)
+    k_classes<double><<<nb, 256, 0, h->stream>>>((const double *)h->R, h->n, h->k, dcls);
+  else
+    k_classes<float><<<nb, 256, 0, h->stream>>>((const float *)h->R, h->n, h->k, dcls);
+  FEM_CUDA(cudaGetLastError());
+  return FEM_OK;
+}
+
+}  // namespace fem

@@ -1,0 +1,155 @@
+// fem_internal.cuh -- shared definitions of the sm_103a EM / k-means library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <random>
+
+#include "../../include/fastem_gpu.h"
+
+namespace fem {
+
+// thread-local message of the last failing call (fem_last_error)
+void set_error(const char *fmt, ...);
+
+#define FEM_CUDA(call)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::fem::set_error("%s:%d %s failed: %s", __FILE__, __LINE__, #call,                \
+                       cudaGetErrorString(e_));                                         \
+      return FEM_ERR_CUDA;                                                              \
+    }                                                                                   \
+  } while (0)
+
+#define FEM_TRY(expr)                 \
+  do {                                \
+    int s_ = (expr);                  \
+    if (s_ != FEM_OK) return s_;      \
+  } while (0)
+
+// Checks that `device` exists and is an sm_103 part; selects it.
+int select_device(int device);
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the live count)
+int sm_count();
+
+template <typename T>
+int dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return FEM_OK;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    *p = nullptr;
+    return FEM_ERR_CUDA;
+  }
+  return FEM_OK;
+}
+
+template <typename T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+// ---------------------------------------------------------------- device status
+// One word per handle on the device.  Kernels never trap: they record what
+// went wrong here and return; the host reads it after the sweep.
+struct DevStatus {
+  double logl;         // sum_i LSE_i of the last E-step
+  int chol_failed;     // first component whose Cholesky pivot was <= 0 (INT_MAX: none)
+  int timeout;         // a bounded wait gave up (mixed-precision kernels)
+  int64_t rechecked;   // k-means rows re-decided in FP64
+  double fit;          // k-means sum of squared distances
+};
+
+// ------------------------------------------------------------------ EM handle
+enum { EM_PAR_CHUNKS = 0 };
+
+struct EmHandle;
+struct TcEmPlan;  // mixed-precision launch plan (em_tc.cu)
+
+}  // namespace fem
+
+struct fem_em {
+  int d = 0, k = 0;
+  int64_t n = 0;
+  fem_em_config cfg{};
+  cudaStream_t stream = nullptr;
+  bool have_data = false, have_params = false, have_post = false, factored = false;
+
+  // dataset
+  float *X = nullptr;                // n x d
+  __nv_bfloat16 *Xhi = nullptr;      // n x d (mixed)
+  __nv_bfloat16 *Xlo = nullptr;      // n x d (mixed)
+
+  // parameters (FP64)
+  double *pi = nullptr, *mu = nullptr, *sigma = nullptr;   // k, k*d, k*d*d
+  double *linv = nullptr;            // k*d*d  L^-1 (lower), row-major
+  double *logdet = nullptr, *logc = nullptr;  // k
+  double *work = nullptr;            // k*d*d  factorisation scratch
+
+  // kernel-side copies: T = double (FP64) or float (FP32 / mixed)
+  void *muT = nullptr, *linvT = nullptr, *logcT = nullptr;
+
+  // posteriors, component-major k x n (T)
+  void *R = nullptr;
+
+  // E-step partials
+  double *logl_part = nullptr;
+  int64_t n_logl_part = 0;
+  // M-step partials (FP64)
+  double *mpart = nullptr;      // means: grid x k x (d+1)
+  int mgrid = 0;
+  double *cpart = nullptr;      // covariances: chunks x k x nblk x 64
+  int cchunks = 0, cunits_blocks = 0;
+  double *psum = nullptr;       // k   PosteriorSum
+
+  // mixed-precision state (em_tc.cu)
+  fem::TcEmPlan *tc = nullptr;
+
+  fem::DevStatus *dstat = nullptr;   // device
+  fem::DevStatus *hstat = nullptr;   // pinned host
+
+  // timing
+  bool timing = false;
+  unsigned tmask = 0;            // event slots recorded since the last sync
+  cudaEvent_t ev[8] = {};
+  double t_estep = 0, t_mstep = 0, t_final = 0;
+  int64_t launches = 0;
+};
+
+struct fem_km {
+  int d = 0, k = 0;
+  int64_t n = 0;
+  fem_km_config cfg{};
+  cudaStream_t stream = nullptr;
+  bool have_data = false;
+  std::mt19937_64 rng;
+  std::uniform_real_distribution<> uni;
+
+  float *X = nullptr;              // n x d
+  __nv_bfloat16 *Xb = nullptr;     // n x d (mixed)
+  float *xnorm = nullptr;          // n   ||x_i|| (mixed bound)
+  int32_t *labels = nullptr;       // n
+  double *cent = nullptr;          // k x d (FP64 centroids, device)
+  float *centf = nullptr;          // k x d float copy
+  __nv_bfloat16 *centb = nullptr;  // k x d bf16 copy (mixed)
+  float *cnorm = nullptr;          // k   ||c_j|| and ||c_j||^2
+  long long *acc = nullptr;        // grid x k x d  fixed-point partial sums
+  int *cnt = nullptr;              // grid x k
+  int grid = 0;
+  int shift = 0;                   // fixed-point scale 2^shift
+  double xg2 = 0.0;                // sum_i ||x_i - g||^2
+  double *g = nullptr;             // data mean (device, d)
+  double *hg = nullptr;            // data mean (host)
+  double *out = nullptr;           // device: k x d new centroids, k counts (as double), fit
+  double *hout = nullptr;          // pinned host copy
+  fem::DevStatus *dstat = nullptr;
+  fem::DevStatus *hstat = nullptr;
+  cudaEvent_t ev[4] = {};
+  double t_assign = 0, t_update = 0;
+};

@@ -1,0 +1,177 @@
+/*
+ * fastem_gpu.h -- C-ABI of the GB300 (sm_103a) EM and k-means hot path.
+ *
+ * The reference exposes this path as C++ virtual methods (no C ABI):
+ *   EMAlgorithm        EM2/EMAlgorithm.h:26-79   (TrainNoCopy, SetParameters,
+ *                      PrecomputeDensityMatrix, MStep, InitDensities, ...)
+ *   SimpleMatrixEM     EM2/MatrixEM.h:83-100
+ *   NormalDensity      EM2/NormalDensity.h:24-57
+ *   KMeansAlgorithm    Clust/KMAlgorithm.h:29-68  (RunKMeans, ComputeMSEAndCorrect)
+ *   NaiveKMA           Clust/KMAlgorithm.h:85-117
+ * A CUDA backend registered beside "matrixem"/"simplematrixem"/"cachedem" in
+ * CreateEMAlgorithm (EM2/EMAlgorithm.cpp:247-269) binds exactly these entry
+ * points; the C++ classes in fastem_gb300/host/ are that binding.
+ *
+ * Conventions: plain pointers and sizes; N is int64_t; every array is
+ * row-major; covariances are K consecutive d*d blocks; all parameters are
+ * double on the host side (the reference's OPTFLOAT is double in every
+ * build that compiles, Util/Optfloat.h:3-9).  Host pointers unless the name
+ * says "device".  Every call returns a fem_status; the reference's
+ * exceptions map as EMException -> FEM_ERR_CHOLESKY / FEM_ERR_COND_ABORT,
+ * std::invalid_argument -> FEM_ERR_BAD_ARG.  A handle owns one CUDA stream
+ * and must be used by one host thread at a time.  There is no CPU fallback:
+ * without a usable CUDA device every create call returns FEM_ERR_NO_DEVICE.
+ */
+#ifndef FASTEM_GPU_H_
+#define FASTEM_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEM_API_VERSION 1
+
+typedef enum fem_status {
+  FEM_OK = 0,
+  FEM_ERR_BAD_ARG = 1,     /* std::invalid_argument in the reference */
+  FEM_ERR_CUDA = 2,        /* a CUDA runtime/driver call failed */
+  FEM_ERR_CHOLESKY = 3,    /* "Cholesky decomposition failed" (EM2/NormalDensity.cpp:48-49) */
+  FEM_ERR_COND_ABORT = 4,  /* "Condition number ... too high" (EM2/EMAlgorithm.cpp:147-151) */
+  FEM_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  FEM_ERR_NO_DEVICE = 6,   /* no CUDA device / not sm_103 */
+  FEM_ERR_STATE = 7,       /* call out of order (e.g. iterate before upload) */
+  FEM_ERR_UNSUPPORTED = 8  /* shape not supported by the requested precision */
+} fem_status;
+
+typedef enum fem_precision {
+  FEM_PREC_FP64 = 0,  /* whole iteration in FP64, like the reference's double build */
+  FEM_PREC_FP32 = 1,  /* whole iteration in FP32 on CUDA cores (plain baseline) */
+  FEM_PREC_MIXED = 2  /* tcgen05 BF16 contractions, FP32 accumulate, FP64 Cholesky/logdet/logL */
+} fem_precision;
+
+/* returns FEM_API_VERSION */
+int fem_api_version(void);
+/* message of the last failing call on this thread (never NULL) */
+const char *fem_last_error(void);
+
+/* ================================ EM ================================= */
+
+typedef struct fem_em fem_em;
+
+typedef struct fem_em_config {
+  int precision;      /* fem_precision */
+  int device;         /* CUDA device ordinal */
+  int max_sweeps;     /* EMAlgorithm::MaxSweeps   (default 1000000, EM2/EMAlgorithm.cpp:41) */
+  double eps;         /* EMAlgorithm::Eps         (default 1e-5,    EM2/EMAlgorithm.cpp:42) */
+  double abort_thr;   /* EMAlgorithm::AbortThr    (default 1e5,     EM2/EMAlgorithm.cpp:43) */
+  double reg_coef;    /* EMAlgorithm::RegCoef     (default 0,       EM2/EMAlgorithm.cpp:44) */
+  int svd;            /* condition-number check per sweep (EM2/EMArgs.cpp:40, default on) */
+} fem_em_config;
+
+/* fills the reference defaults (precision FEM_PREC_MIXED, device 0) */
+void fem_em_config_default(fem_em_config *cfg);
+
+/* EMAlgorithm / SimpleMatrixEM constructor (EM2/EMAlgorithm.cpp:32-64,
+ * EM2/MatrixEM.cpp:259-273): sizes every device buffer for n rows, d
+ * columns and k components.  Replaces CreateEMAlgorithm("simplematrixem",
+ * ...) (EM2/EMAlgorithm.cpp:247-269). */
+int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **out);
+void fem_em_destroy(fem_em *h);
+
+/* EMAlgorithm::SetParameters (EM2/EMAlgorithm.cpp:25-30) */
+int fem_em_set_parameters(fem_em *h, int max_sweeps, double eps, double abort_thr,
+                          double reg_coef);
+
+/* EMAlgorithm::CopyDataset / MatrixEM::CopyDataset (EM2/EMAlgorithm.cpp:225-235,
+ * EM2/MatrixEM.cpp:102-121): float rows (ld floats apart) -> device. */
+int fem_em_upload(fem_em *h, const float *X, int64_t ld);
+/* same, from device memory (rows already resident in HBM) */
+int fem_em_upload_device(fem_em *h, const float *dX, int64_t ld);
+
+/* EMAlgorithm::DecodeMixture (EM2/EMAlgorithm.cpp:125-131): pi[k], mu[k*d],
+ * sigma[k*d*d] (the lower triangle is used, EM2/NormalDensity.cpp:45). */
+int fem_em_set_params(fem_em *h, const double *pi, const double *mu, const double *sigma);
+/* GaussianMixture::Init target of TrainNoCopy (EM2/EMAlgorithm.cpp:186-189) */
+int fem_em_get_params(fem_em *h, double *pi, double *mu, double *sigma);
+
+/* EMAlgorithm::TrainNoCopy (EM2/EMAlgorithm.cpp:139-191): regularise,
+ * factor, optional condition check, then sweeps until |dL/L| < Eps or
+ * MaxSweeps.  logl_trace / e_trace (capacity entries each, may be NULL)
+ * receive the per-sweep LogL and e; *iter_counter is IterCounter after the
+ * loop; *logl the returned LogL (computed before the last M-step). */
+int fem_em_train(fem_em *h, int svd, double *logl_trace, double *e_trace, int capacity,
+                 int *iter_counter, double *logl);
+
+/* Single pieces of one sweep, for hosts that drive the loop themselves:
+ * EMAlgorithm::InitDensities after RegularizeCovariances
+ * (EM2/EMAlgorithm.cpp:75-87,237-244); status FEM_ERR_CHOLESKY with the
+ * failing component in *failed. */
+int fem_em_init_densities(fem_em *h, int *failed);
+/* SimpleMatrixEM::PrecomputeDensityMatrix + ComputeLogLike
+ * (EM2/MatrixEM.cpp:275-307): posteriors on device, returns sum_i LSE_i */
+int fem_em_precompute(fem_em *h, double *logl);
+/* SimpleMatrixEM::MStep (EM2/MatrixEM.cpp:309-378) */
+int fem_em_mstep(fem_em *h);
+/* EMAlgorithm::FindLargestConditionNumber (EM2/EMAlgorithm.cpp:193-202) */
+int fem_em_max_condition(fem_em *h, double *cond);
+
+/* EMAlgorithm::Posteriors (EM2/EMAlgorithm.h:41) after the last E-step, as
+ * an n x k row-major double matrix. */
+int fem_em_get_posteriors(fem_em *h, double *post);
+/* EMAlgorithm::RetrieveClasses (EM2/EMAlgorithm.cpp:107-122) */
+int fem_em_retrieve_classes(fem_em *h, int32_t *classes);
+/* NormalDensity::GetInvertedCholCov / GetLogDeterminant
+ * (EM2/NormalDensity.h:42,45): U_j = (L_j^-1)^T upper, k*d*d, and logdet[k] */
+int fem_em_get_factors(fem_em *h, double *U, double *logdet);
+
+/* Device time (ms, CUDA events on the handle's stream) of the E-step and
+ * M-step kernels over the last `fem_em_timing_reset` window, and launch
+ * counts. */
+int fem_em_timing_reset(fem_em *h, int enable);
+int fem_em_timing_get(fem_em *h, double *estep_ms, double *mstep_ms, double *finalize_ms,
+                      int64_t *launches);
+
+/* ============================== k-means ============================== */
+
+typedef struct fem_km fem_km;
+
+typedef struct fem_km_config {
+  int precision;   /* FEM_PREC_FP32 (CUDA-core distances) or FEM_PREC_MIXED (tcgen05 BF16) */
+  int device;
+  uint64_t seed;   /* seed of the repair RNG (Util/Rand.cpp SRand) */
+  int repair;      /* 1: CentroidRandomRepair (Clust/CentroidRepair.cpp:21-28); 0: leave empty */
+} fem_km_config;
+
+void fem_km_config_default(fem_km_config *cfg);
+
+/* NaiveKMA constructor (Clust/KMAlgorithm.cpp:102-115) */
+int fem_km_create(int d, int64_t n, int k, const fem_km_config *cfg, fem_km **out);
+void fem_km_destroy(fem_km *h);
+/* rows of the MultithreadedDataset the reference iterates over */
+int fem_km_upload(fem_km *h, const float *X, int64_t ld);
+int fem_km_upload_device(fem_km *h, const float *dX, int64_t ld);
+/* NaiveKMA::InitDataStructures (Clust/KMAlgorithm.cpp:140-146) */
+int fem_km_init_data_structures(fem_km *h);
+/* NaiveKMA::ComputeMSEAndCorrect (Clust/KMAlgorithm.cpp:205-255):
+ * centroids (k*d double, CentroidVector layout Clust/CentroidVector.h:11-17)
+ * updated in place; *fit = sum of squared distances / N; counts[k] may be
+ * NULL.  Assignments are bit-exact to an FP64 difference-form argmin with
+ * the lowest index winning ties. */
+int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, int64_t *counts);
+/* KMeansAlgorithm::RunKMeans (Clust/KMAlgorithm.cpp:44-87) */
+int fem_km_run(fem_km *h, double *centroids, double min_rel, int max_iter, double *best_fit,
+               int *iters);
+/* assignment of every row after the last iteration */
+int fem_km_get_assignment(fem_km *h, int32_t *labels);
+/* reseed the repair RNG (SRand, Util/Rand.cpp:33-35) */
+int fem_km_seed(fem_km *h, uint64_t seed);
+/* diagnostics: rows re-decided in FP64 and kernel time of the last iteration */
+int fem_km_stats(fem_km *h, int64_t *rechecked_rows, double *assign_ms, double *update_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTEM_GPU_H_ */

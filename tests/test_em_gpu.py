@@ -1,0 +1,155 @@
+"""GPU parity of the EM sweep (FP64 and FP32 CUDA-core forms) against the
+FP64 oracle, through the C-ABI."""
+import numpy as np
+import pytest
+
+from fastem_gb300 import CudaMatrixEM, GaussianMixture, synth
+from fastem_gb300 import _capi as C
+
+pytestmark = pytest.mark.gpu
+
+
+def small_case(oracle, seed=7, n=20000, d=8, k=6, init_seed=2):
+    X, _ = synth.em_small(seed=seed, n=n, d=d, k=k)
+    oracle.rng_seed(init_seed)
+    return X, synth.identity_init(oracle.kmeans_plusplus(X, k))
+
+
+def run_gpu(X, init, sweeps, precision, eps=0.0, reg=0.0):
+    n, d = X.shape
+    k = len(init[0])
+    with CudaMatrixEM(d, n, k, precision=precision) as em:
+        em.SetParameters(sweeps, eps, 1e5, reg)
+        G = GaussianMixture(*init)
+        ll = em.Train(X, G, svd=False)
+        return dict(logl=em.logl_trace.copy(), e=em.e_trace.copy(), iters=em.GetIterCounter(),
+                    final=ll, pi=G.weights, mu=G.means, sigma=G.covs)
+
+
+def test_em_fp64_config1_50_sweeps(gpu_lib, oracle):
+    """N=100,000, d=8, K=10, seed 1, k-means++ (seed 2) means, identity
+    covariances, uniform weights; 50 sweeps; per-sweep logL vs the oracle."""
+    X, _ = synth.em_small()
+    n = len(X)
+    oracle.rng_seed(2)
+    init = synth.identity_init(oracle.kmeans_plusplus(X, 10))
+    ref = oracle.em_train(X, *init, 50, eps=0.0)
+    got = run_gpu(X, init, 50, "fp64")
+    assert len(got["logl"]) == 50 and got["iters"] == ref["iter_counter"]
+    # tolerance: FP64 with a different summation order
+    assert np.max(np.abs(got["logl"] - ref["logl"])) / n <= 1e-10
+    np.testing.assert_allclose(got["pi"], ref["pi"], rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(got["mu"], ref["mu"], rtol=1e-8, atol=1e-9)
+    np.testing.assert_allclose(got["sigma"], ref["sigma"], rtol=1e-7, atol=1e-9)
+
+
+def test_em_fp64_golden_fixture(gpu_lib):
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "em_small.npz"))
+    got = run_gpu(z["X"], (z["pi0"], z["mu0"], z["sigma0"]), 12, "fp64")
+    np.testing.assert_allclose(got["logl"], z["logl"], rtol=1e-11)
+    np.testing.assert_allclose(got["mu"], z["mu"], rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(got["sigma"], z["sigma"], rtol=1e-9, atol=1e-10)
+
+
+def test_em_fp32_plain_against_fp64(gpu_lib, oracle):
+    """FP32 CUDA-core sweep on an em_large-shaped case (d=64)."""
+    X, _ = synth.em_large(seed=3, n=1 << 16, d=64, k=16)
+    init = synth.forgy_init(X, 16, seed=5)
+    ref = oracle.em_train(X, *init, 5, eps=0.0)
+    got = run_gpu(X, init, 5, "fp32")
+    err = np.max(np.abs(got["logl"] - ref["logl"])) / len(X)
+    print("fp32 plain |dlogL/N| =", err)
+    # tolerance of the FP32 form (per-point terms in FP32, sums in FP64)
+    assert err <= 2e-4
+
+
+def test_em_pieces_match_oracle(gpu_lib, oracle):
+    """InitDensities / PrecomputeDensityMatrix / MStep one by one."""
+    X, init = small_case(oracle)
+    n, d = X.shape
+    k = len(init[0])
+    with CudaMatrixEM(d, n, k, precision="fp64") as em:
+        em.CopyDataset(X)
+        em.SetMixture(GaussianMixture(*init))
+        em.InitDensities()
+        U, ld = em.Factors()
+        st, Uo, ldo, _ = oracle.init_densities(init[2])
+        np.testing.assert_allclose(U, Uo, rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(ld, ldo, rtol=1e-12, atol=1e-14)
+        ll = em.PrecomputeDensityMatrix()
+        post_o, ll_o = oracle.estep(X, init[0], init[1], Uo, ldo)
+        assert abs(ll - ll_o) <= 1e-12 * abs(ll_o)
+        post = em.Posteriors()
+        np.testing.assert_allclose(post, post_o, rtol=1e-11, atol=1e-13)
+        cls = em.RetrieveClasses()
+        assert np.array_equal(cls, np.argmax(post_o, axis=1))
+        em.MStep()
+        G = em.GetMixture()
+        pi, mu, sg = oracle.mstep(X, post_o)
+        np.testing.assert_allclose(G.weights, pi, rtol=1e-11)
+        np.testing.assert_allclose(G.means, mu, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(G.covs, sg, rtol=1e-9, atol=1e-11)
+
+
+@pytest.mark.parametrize("n", [1, 127, 129, 4097])
+def test_em_ragged_sizes(gpu_lib, oracle, n):
+    X, _ = synth.em_small(seed=21, n=max(n, 1), d=4, k=2)
+    X = X[:n]
+    init = (np.array([0.5, 0.5]), X[[0, 0]].astype(np.float64) + np.array([[0.0] * 4, [1.0] * 4]),
+            np.stack([np.eye(4) * 4.0] * 2))
+    ref = oracle.em_train(X, *init, 1, eps=0.0)
+    got = run_gpu(X, init, 1, "fp64")
+    assert abs(got["logl"][0] - ref["logl"][0]) <= 1e-11 * abs(ref["logl"][0])
+
+
+def test_em_single_component_closed_form(gpu_lib):
+    """K=1: one sweep gives the sample mean and the (biased) sample covariance."""
+    rng = np.random.default_rng(0)
+    X = (rng.standard_normal((5000, 8)) @ rng.standard_normal((8, 8)) + 3.0).astype(np.float32)
+    got = run_gpu(X, (np.ones(1), np.zeros((1, 8)), np.eye(8)[None] * 10.0), 1, "fp64")
+    Xd = X.astype(np.float64)
+    m = Xd.mean(axis=0)
+    np.testing.assert_allclose(got["mu"][0], m, rtol=1e-11, atol=1e-11)
+    np.testing.assert_allclose(got["sigma"][0], (Xd - m).T @ (Xd - m) / len(X), rtol=1e-10, atol=1e-11)
+    assert got["pi"][0] == pytest.approx(1.0, abs=1e-14)
+
+
+def test_em_convergence_iter_counter(gpu_lib, oracle):
+    X, init = small_case(oracle, seed=9, n=8000, d=4, k=3)
+    ref = oracle.em_train(X, *init, 500, eps=1e-6)
+    got = run_gpu(X, init, 500, "fp64", eps=1e-6)
+    assert got["iters"] == ref["iter_counter"]
+    assert abs(got["final"] - ref["final_logl"]) <= 1e-10 * abs(ref["final_logl"])
+
+
+def test_em_regularized(gpu_lib, oracle):
+    X, init = small_case(oracle, seed=10, n=6000, d=8, k=4)
+    ref = oracle.em_train(X, *init, 6, eps=0.0, reg_coef=0.01)
+    got = run_gpu(X, init, 6, "fp64", reg=0.01)
+    np.testing.assert_allclose(got["logl"], ref["logl"], rtol=1e-11)
+
+
+def test_em_cholesky_failure_is_reported(gpu_lib):
+    X, _ = synth.em_small(seed=3, n=1000, d=4, k=2)
+    bad = np.stack([np.eye(4), np.diag([1.0, -1.0, 1.0, 1.0])])
+    with CudaMatrixEM(4, 1000, 2, precision="fp64") as em:
+        em.CopyDataset(X)
+        em.SetParameters(3, 0.0, 1e5)
+        with pytest.raises(C.CholeskyError) as ei:
+            em.TrainNoCopy(GaussianMixture(np.array([0.5, 0.5]), X[:2], bad))
+        assert "component 1" in str(ei.value)
+        # the handle stays usable
+        ok = np.stack([np.eye(4)] * 2)
+        em.TrainNoCopy(GaussianMixture(np.array([0.5, 0.5]), X[:2].astype(np.float64), ok))
+
+
+def test_em_condition_abort(gpu_lib):
+    X, _ = synth.em_small(seed=4, n=2000, d=4, k=2)
+    ill = np.stack([np.eye(4), np.diag([1e-4, 1.0, 1.0, 10.0])])
+    with CudaMatrixEM(4, 2000, 2, precision="fp64") as em:
+        em.CopyDataset(X)
+        em.SetParameters(3, 0.0, 1e5)
+        with pytest.raises(C.ConditionAbort):
+            em.TrainNoCopy(GaussianMixture(np.array([0.5, 0.5]), X[:2].astype(np.float64), ill), svd=True)
+        assert em.FindLargestConditionNumber() == pytest.approx(1e5, rel=1e-9)

@@ -1,0 +1,100 @@
+"""GPU parity of the Lloyd iteration: assignments bit-exact to the FP64
+oracle, centroids and fit within FP64 rounding."""
+import os
+
+import numpy as np
+import pytest
+
+from fastem_gb300 import CudaKMA, synth
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def iterate_both(oracle, X, C0, iters, precision, repair=True, seed=0):
+    n, d = X.shape
+    k = C0.shape[0]
+    Cg = np.array(C0, dtype=np.float64, copy=True)
+    Co = Cg.copy()
+    out = []
+    with CudaKMA(d, n, k, precision=precision, seed=seed, repair=repair) as km:
+        km.SetDataset(X)
+        oracle.rng_seed(seed)
+        for _ in range(iters):
+            fg, cg = km.ComputeMSEAndCorrectCounts(Cg)
+            lg = km.Assignment()
+            fo, Co, co, lo = oracle.km_iterate(X, Co, repair=repair)
+            out.append((fg, cg, lg, Cg.copy(), fo, co, lo, Co.copy(), km.Stats()))
+    return out
+
+
+def check_iters(out):
+    for it, (fg, cg, lg, Cg, fo, co, lo, Co, st) in enumerate(out):
+        assert np.array_equal(lg, lo), "labels differ at iteration %d (%d rows)" % (it, (lg != lo).sum())
+        assert np.array_equal(cg, co)
+        assert abs(fg - fo) <= 1e-11 * abs(fo)
+        np.testing.assert_allclose(Cg, Co, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("precision", ["fp32"])
+def test_km_blobs_30_iterations(gpu_lib, oracle, precision):
+    """kmeans_blobs shape at reduced N (d=32, K=64), k-means|| seed 3, 30 iterations."""
+    X, _ = synth.kmeans_blobs(seed=2, n=1 << 17, d=32, k=64)
+    C0 = oracle.kmeans_oror(X, 64, seed=3)
+    out = iterate_both(oracle, X, C0, 30, precision)
+    check_iters(out)
+    print("rechecked rows per iteration:", [o[-1]["rechecked"] for o in out])
+
+
+@pytest.mark.parametrize("precision", ["fp32"])
+def test_km_golden_fixture(gpu_lib, precision):
+    z = np.load(os.path.join(GOLDEN, "km_blobs.npz"))
+    C = z["C0"].copy()
+    with CudaKMA(8, len(z["X"]), 8, precision=precision) as km:
+        km.SetDataset(z["X"])
+        for it in range(len(z["fits"])):
+            fit, cnt = km.ComputeMSEAndCorrectCounts(C)
+            assert np.array_equal(km.Assignment(), z["labels"][it])
+            assert np.array_equal(cnt, z["counts"][it])
+            assert abs(fit - z["fits"][it]) <= 1e-12 * z["fits"][it]
+            np.testing.assert_allclose(C, z["centroids"][it], rtol=1e-14, atol=1e-14)
+
+
+def test_km_exact_ties_lowest_index(gpu_lib):
+    z = np.load(os.path.join(GOLDEN, "km_ties.npz"))
+    C = z["C0"].copy()
+    with CudaKMA(2, len(z["X"]), 4, precision="fp32", repair=False) as km:
+        km.SetDataset(z["X"])
+        fit, cnt = km.ComputeMSEAndCorrectCounts(C)
+        assert np.array_equal(km.Assignment(), z["labels"])
+        assert np.array_equal(cnt, z["counts"])
+        assert km.Stats()["rechecked"] >= 2
+
+
+def test_km_empty_cluster_repair(gpu_lib, oracle):
+    X, _ = synth.kmeans_blobs(seed=6, n=1000, d=4, k=3)
+    C0 = np.vstack([X[:3].astype(np.float64), np.full((1, 4), 1e6)])
+    out = iterate_both(oracle, X, C0, 2, "fp32", seed=17)
+    assert out[0][1][3] == 0
+    check_iters(out)
+
+
+@pytest.mark.parametrize("n", [1, 255, 257, 10001])
+def test_km_ragged(gpu_lib, oracle, n):
+    X, _ = synth.kmeans_blobs(seed=8, n=max(n, 16), d=16, k=5)
+    X = X[:n]
+    C0 = X[np.arange(5) % n].astype(np.float64) + 0.5
+    check_iters(iterate_both(oracle, X, C0, 2, "fp32", repair=False))
+
+
+def test_km_run_matches_oracle(gpu_lib, oracle):
+    X, _ = synth.kmeans_blobs(seed=4, n=30000, d=8, k=10)
+    C0 = oracle.kmeans_forgy(X, 10, seed=1)
+    best_o, Co, it_o = oracle.km_run(X, C0, min_rel=1e-4, max_iter=30)
+    Cg = C0.copy()
+    with CudaKMA(8, len(X), 10, precision="fp32") as km:
+        km.SetDataset(X)
+        best_g = km.RunKMeans(Cg, MinRel=1e-4, MaxIter=30)
+        assert km.IterCount == it_o
+    assert abs(best_g - best_o) <= 1e-11 * best_o
+    np.testing.assert_allclose(Cg, Co, rtol=1e-13, atol=1e-13)
