@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 #include <random>
@@ -83,8 +84,8 @@ struct fem_em {
 
   // dataset
   float *X = nullptr;                // n x d
-  __nv_bfloat16 *Xhi = nullptr;      // n x d (mixed)
-  __nv_bfloat16 *Xlo = nullptr;      // n x d (mixed)
+  __half *Xhi = nullptr;             // n x d  fp16(x)        (mixed)
+  __half *Xlo = nullptr;             // n x d  fp16(x - xhi)  (mixed)
 
   // parameters (FP64)
   double *pi = nullptr, *mu = nullptr, *sigma = nullptr;   // k, k*d, k*d*d

@@ -136,6 +136,25 @@ def forgy_init(X, k, seed):
     return identity_init(X[rows].astype(np.float64))
 
 
+def dsquared_init(X, k, seed, sample=1 << 16):
+    """Means by D^2 sampling (k-means++ rule) on a seeded row sample, with
+    identity covariances and uniform weights.  A harness initialisation:
+    numpy-seeded, cheap at any N (the reference's own seeders with its
+    mt19937_64 stream live in the oracle and the C++ host library)."""
+    rng = np.random.default_rng(seed)
+    n, d = X.shape
+    idx = rng.choice(n, size=min(n, sample), replace=False)
+    S = X[idx].astype(np.float64)
+    means = np.empty((k, d))
+    means[0] = S[rng.integers(len(S))]
+    dist = ((S - means[0]) ** 2).sum(axis=1)
+    for i in range(1, k):
+        p = dist / dist.sum()
+        means[i] = S[rng.choice(len(S), p=p)]
+        dist = np.minimum(dist, ((S - means[i]) ** 2).sum(axis=1))
+    return identity_init(means)
+
+
 def identity_init(means):
     k, d = means.shape
     return (np.full(k, 1.0 / k), np.array(means, dtype=np.float64, copy=True),

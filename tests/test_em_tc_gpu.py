@@ -1,0 +1,51 @@
+"""GPU parity of the mixed-precision (tcgen05, FP16x3 / FP32-accumulate /
+FP64 factorisation) EM path against the FP64 oracle.
+
+Tolerance: |dlogL/N| <= 1e-5 per sweep (the precision target of the mixed
+form); E-step alone <= 1e-6; posteriors within 1e-4 absolute."""
+import numpy as np
+import pytest
+
+from fastem_gb300 import CudaMatrixEM, GaussianMixture, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def estep_case(oracle, n, k, seed=3):
+    X, _ = synth.em_large(seed=seed, n=n, d=64, k=k)
+    init = synth.dsquared_init(X, k, seed=5)
+    st, U, ld, _ = oracle.init_densities(init[2])
+    post_o, ll_o = oracle.estep(X, init[0], init[1], U, ld)
+    return X, init, post_o, ll_o
+
+
+@pytest.mark.parametrize("n,k", [(1 << 15, 16), (4096 + 77, 128), (100, 8), (128, 4)])
+def test_tc_estep_matches_oracle(gpu_lib, oracle, n, k):
+    X, init, post_o, ll_o = estep_case(oracle, n, k)
+    with CudaMatrixEM(64, n, k, precision="mixed") as em:
+        em.CopyDataset(X)
+        em.SetMixture(GaussianMixture(*init))
+        em.InitDensities()
+        ll = em.PrecomputeDensityMatrix()
+        post = em.Posteriors()
+    err = abs(ll - ll_o) / n
+    print("tc E-step n=%d k=%d |dlogL/N| = %.3g, max |dr| = %.3g" % (n, k, err, np.abs(post - post_o).max()))
+    assert err <= 1e-6
+    assert np.abs(post - post_o).max() <= 1e-4
+
+
+def test_tc_sweeps_em_large_shape(gpu_lib, oracle):
+    """em_large shape (d=64) at N=2^17, K=32: 8 sweeps, per-sweep logL."""
+    n, k = 1 << 17, 32
+    X, _ = synth.em_large(seed=3, n=n, d=64, k=k)
+    init = synth.dsquared_init(X, k, seed=5)
+    ref = oracle.em_train(X, *init, 8, eps=0.0)
+    with CudaMatrixEM(64, n, k, precision="mixed") as em:
+        em.SetParameters(8, 0.0, 1e5)
+        G = GaussianMixture(*init)
+        em.Train(X, G)
+        ll = em.logl_trace
+    err = np.abs(ll - ref["logl"]) / n
+    print("tc sweeps |dlogL/N| per sweep:", " ".join("%.2e" % e for e in err))
+    assert err.max() <= 1e-5
+    np.testing.assert_allclose(G.weights, ref["pi"], rtol=1e-4, atol=1e-7)
