@@ -96,7 +96,7 @@ def build_gpu(verbose=False, jobs=None, extra_flags=()):
         for f in futs:
             f.result()
     if todo or not os.path.exists(GPU_LIB) or os.path.getmtime(GPU_LIB) < _newest(objs):
-        _run([cc] + ARCH + ["-shared", "-o", GPU_LIB] + objs + ["-lcuda"], verbose)
+        _run([cc] + ARCH + ["-shared", "-o", GPU_LIB] + objs, verbose)
     return GPU_LIB
 
 

@@ -308,21 +308,8 @@ __global__ void k_reduce_parts(const double *__restrict__ part, int np, DevStatu
 // ==================================================== host: tensor maps
 static int encode_2d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
                      uint32_t box_rows) {
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {box_cols, box_rows};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = cuTensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims,
-                                      strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    const char *msg = nullptr;
-    cuGetErrorString(r, &msg);
-    set_error("cuTensorMapEncodeTiled failed: %s", msg ? msg : "?");
-    return FEM_ERR_CUDA;
-  }
-  return FEM_OK;
+  return encode_tmap_2d(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, cols, rows, box_cols, box_rows,
+                        CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 static size_t esmem_bytes() { return sizeof(ESmem) + 1024; }

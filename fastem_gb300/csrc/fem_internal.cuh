@@ -1,6 +1,7 @@
 // fem_internal.cuh -- shared definitions of the sm_103a EM / k-means library.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -33,6 +34,10 @@ void set_error(const char *fmt, ...);
 
 // Checks that `device` exists and is an sm_103 part; selects it.
 int select_device(int device);
+
+// 2-D row-major tensor map (cols contiguous), resolved without linking libcuda
+int encode_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, const void *base, uint64_t cols,
+                   uint64_t rows, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz);
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the live count)
 int sm_count();
