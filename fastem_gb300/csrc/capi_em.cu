@@ -204,8 +204,11 @@ int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **ou
       (st = dalloc(&h->logc, k)) || (st = dalloc(&h->work, kdd)) || (st = dalloc(&h->psum, k)) ||
       (st = dalloc(&h->dstat, 1)))
     return fail(st);
+  // posteriors: k x n in T for the CUDA-core forms; the mixed form keeps FP16 hi/lo pairs
+  const size_t rbytes = (c.precision == FEM_PREC_MIXED) ? 0 : (size_t)k * n * ts;
   if (cudaMalloc(&h->muT, kd * ts) != cudaSuccess || cudaMalloc(&h->linvT, kdd * ts) != cudaSuccess ||
-      cudaMalloc(&h->logcT, k * ts) != cudaSuccess || cudaMalloc(&h->R, (size_t)k * n * ts) != cudaSuccess) {
+      cudaMalloc(&h->logcT, k * ts) != cudaSuccess ||
+      (rbytes && cudaMalloc(&h->R, rbytes) != cudaSuccess)) {
     set_error("cudaMalloc failed for the %zu-byte posterior matrix or factors", (size_t)k * n * ts);
     return fail(FEM_ERR_CUDA);
   }
@@ -428,7 +431,7 @@ int fem_em_get_posteriors(fem_em *h, double *post) {
   int st = FEM_OK;
   for (int64_t r0 = 0; r0 < h->n && st == FEM_OK; r0 += chunk) {
     const int64_t rows = std::min(chunk, h->n - r0);
-    st = em_post_rows(h, r0, rows, buf);
+    st = mixed(h) ? em_tc_post_rows(h, r0, rows, buf) : em_post_rows(h, r0, rows, buf);
     if (st == FEM_OK &&
         cudaMemcpyAsync(post + r0 * h->k, buf, (size_t)rows * h->k * sizeof(double),
                         cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
@@ -448,7 +451,7 @@ int fem_em_retrieve_classes(fem_em *h, int32_t *classes) {
   }
   int32_t *dc = nullptr;
   FEM_TRY(dalloc(&dc, h->n));
-  int st = em_classes(h, dc);
+  int st = mixed(h) ? em_tc_classes(h, dc) : em_classes(h, dc);
   if (st == FEM_OK &&
       cudaMemcpyAsync(classes, dc, h->n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
     st = FEM_ERR_CUDA;

@@ -52,7 +52,8 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapFloatOOBfill);
 
 int encode_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, const void *base, uint64_t cols,
-                   uint64_t rows, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz) {
+                   uint64_t rows, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz,
+                   uint64_t pitch_bytes) {
   static EncodeTiledFn fn = nullptr;
   if (!fn) {
     void *p = nullptr;
@@ -66,7 +67,7 @@ int encode_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, const
     fn = (EncodeTiledFn)p;
   }
   cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols * (uint64_t)elem_bytes};
+  cuuint64_t strides[1] = {pitch_bytes ? pitch_bytes : cols * (uint64_t)elem_bytes};
   cuuint32_t box[2] = {box_cols, box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(m, dt, 2, const_cast<void *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,

@@ -1,27 +1,38 @@
-// em_tc.cu -- tcgen05 mixed-precision EM sweep for sm_103a.
+// em_tc.cu -- tcgen05 mixed-precision EM sweep for sm_103a (d = 64).
 //
-// E-step (MatrixEMBase::BlockDensities + PostProcessDensityMatrix,
-// EM2/MatrixEM.cpp:39-51,69-81) as ONE tensor-core GEMM of each 128-point
-// tile against the stacked inverse Cholesky factors of all components:
-//   Y = X W^T,  W = [L_1^-1; ...; L_K^-1]  (K*d x d),  y_jk = (L_j^-1 x)_k
-// in FP16 x 3 (x = xh + xl, W = Wh + Wl: Xh Wh^T + Xh Wl^T + Xl Wh^T) with
-// FP32 accumulation in TMEM.  The epilogue subtracts b_j = L_j^-1 mu_j,
-// squares and sums each component's d columns, adds the log coefficient,
-// keeps an online log-sum-exp per point and writes l_ij, then the
-// posteriors r_ij = exp(l_ij - LSE_i).  The per-point log-likelihood is
-// accumulated in FP64 with the FP64 log coefficient of the winning
-// component (a float coefficient would bias every point of a component by
-// the same rounding error).
+// One sweep = SimpleMatrixEM::PrecomputeDensityMatrix + MStep
+// (EM2/MatrixEM.cpp:275-378) as three tensor-core kernels and two FP64
+// finalisers:
 //
-// Within a group of 4 components the 256 accumulator columns are ordered
-// by 16-wide k-block, highest first, so K-step kb (m in [16kb, 16kb+16))
-// only needs the first 256-64kb columns: the lower-triangular structure of
-// L^-1 skips 37.5% of the MMA work.
+//  1. E-step (MatrixEMBase::BlockDensities + PostProcessDensityMatrix,
+//     EM2/MatrixEM.cpp:39-51,69-81): ONE GEMM of each 128-point tile against
+//     the stacked inverse Cholesky factors of all components,
+//       Y = X W^T,  W = [L_1^-1; ...; L_K^-1],  y_jk = (L_j^-1 x)_k,
+//     in FP16 x 3 (x = xh + xl, W = Wh + Wl: Xh Wh^T + Xh Wl^T + Xl Wh^T)
+//     with FP32 accumulation in TMEM.  The epilogue subtracts b_j = L_j^-1
+//     mu_j, squares and sums each component's 64 columns, adds the log
+//     coefficient and keeps an online log-sum-exp per point; the
+//     posteriors r_ij = exp(l_ij - LSE_i) are stored as FP16 hi/lo pairs
+//     (component-major).  The per-point log-likelihood is summed in FP64
+//     with the FP64 log coefficient of the winning component.
+//     Within a group of 4 components the 256 accumulator columns are
+//     ordered by 16-wide k-block, highest first, so K-step kb only needs
+//     the first 256-64kb columns (L^-1 is lower triangular): 37.5% of the
+//     MMA work is skipped.
+//  2. Means (doMStep means part, EM2/MatrixEM.cpp:319-343): S2 = R^T X and
+//     S1 = R^T 1 as one GEMM per 64-point block, A = [Rh | Rl] (components
+//     x points), B = [Xh^T; 1] / [Xl^T; 0] (80 rows x points); FP32 in TMEM,
+//     flushed to FP64 every 4096 points.
+//  3. Covariances (ComputeWeightedTempDataset + BlockCovariances,
+//     EM2/MatrixEM.cpp:53-67,90-99) around the NEW means: producer warps
+//     form z = sqrt(r) (x - mu_j) in FP32, store fp16(z) as the operand of
+//     an M=128 (two components) x N=128 x K=16 MMA whose diagonal blocks are
+//     Z_j^T Z_j, and accumulate the exact diagonal sum z^2 in FP32 -> FP64
+//     (FP16 rounding would bias the diagonal upward by E[delta^2]).
 //
-// Warp roles (192 threads, one CTA per SM, persistent over tiles):
-//   warp 0      TMA producer (X tile pair per tile, W group pair per group)
-//   warp 1      TMEM owner + single-thread MMA issuer
-//   warps 2..5  epilogue, one TMEM lane (= one point) per thread
+// Every mbarrier wait is bounded; a timeout sets a status word, the roles
+// leave their loops, in-flight copies and MMAs are drained and TMEM is
+// released.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -41,13 +52,16 @@ using namespace tc;
 
 // ------------------------------------------------------------ constants
 constexpr int kD = 64;                   // dimension handled by the tensor-core path
-constexpr int kTileM = 128;              // points per tile
-constexpr int kGroupN = 256;             // accumulator columns per component group
+constexpr int kTileM = 128;              // E-step points per tile
+constexpr int kGroupN = 256;             // E-step accumulator columns per component group
 constexpr int kCompPerGroup = kGroupN / kD;
 constexpr int kXStages = 2, kWStages = 2;
 constexpr uint32_t kXBytes = kTileM * kD * 2;    // one FP16 X tile (16 KB)
 constexpr uint32_t kWBytes = kGroupN * kD * 2;   // one FP16 W group (32 KB)
 constexpr int kEThreads = 192;
+constexpr int kBlk = 64;                 // M-step points per block (one 128-byte swizzle row)
+constexpr int kFlushBlocks = 64;         // FP32 TMEM window: 64 blocks = 4096 points
+constexpr int kMaxK = 128;               // components handled by one means M-tile
 
 struct __align__(1024) ESmem {
   __half xh[kXStages][kTileM * kD];
@@ -62,22 +76,59 @@ struct __align__(1024) ESmem {
   double red[4];
 };
 
+// means kernel: A = Rh/Rl (128 comps x 64 points), B = [X^T; 1] (80 x 64)
+constexpr int kMeanN = 80;
+struct __align__(1024) MSmem {
+  __half rh[2][kMaxK * kBlk];
+  __half rl[2][kMaxK * kBlk];
+  __half bh[2][kMeanN * kBlk];   // rows 0..63 X_h^T, row 64 ones, rows 65..79 zero
+  __half bl[2][kMeanN * kBlk];   // rows 0..63 X_l^T, rows 64..79 zero
+  uint64_t in_full[2], in_empty[2], acc_full[2], acc_empty[2], mma_done;
+  uint32_t tmem_base;
+};
+
+// covariance kernel: 4 components per CTA (2 pairs), 64-point blocks
+struct __align__(1024) CSmem {
+  __half z[2][2][128 * kBlk];    // [stage][pair] 128 rows (comp q dims) x 64 points, SW128
+  float xs[2][kBlk * kD];        // X tile (points x dims)
+  __half rh[2][4 * kBlk];
+  __half rl[2][4 * kBlk];
+  float sr[2][4 * kBlk];         // sqrt(r)
+  uint64_t in_full[2], in_empty[2], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
+  uint32_t tmem_base;
+};
+constexpr int kCThreads = 448;   // warp 0 TMA, 1 MMA, 2..9 producers, 10..13 flush
+
 struct TcEmPlan {
-  CUtensorMap tm_xh, tm_xl, tm_wh, tm_wl;
+  CUtensorMap tm_xh, tm_xl, tm_wh, tm_wl;      // E-step
+  CUtensorMap tm_rh, tm_rl, tm_xht, tm_xlt;    // means
+  CUtensorMap tm_x32, tm_rh4, tm_rl4;          // covariances
   __half *Wh = nullptr, *Wl = nullptr;  // (K*d) x d, permuted rows
   float *bias = nullptr;                // K*d, permuted
+  __half *Rh = nullptr, *Rl = nullptr;  // K x np posteriors hi / lo
+  __half *XhT = nullptr, *XlT = nullptr;  // d x np
+  int64_t np = 0;                       // padded row pitch (multiple of 64)
+  float *lsc = nullptr;                 // E-step scratch: egrid x K x 128
   double *epart = nullptr;              // per-CTA log-likelihood
+  double *mpart = nullptr;              // means partials: mgrid x 128 x 80
+  double *cpart = nullptr;              // covariance partials: cgrid x 4 x 64 x 64
+  double *dpart = nullptr;              // exact diagonals: cgrid x 4 x 64
+  float *muf = nullptr;                 // new means (float) for the covariance producers
   int *err = nullptr;                   // device status of the bounded waits
-  int egrid = 0;
+  int egrid = 0, mgrid = 0, cgx = 0, cgy = 0;
 };
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 // ============================================================== E-step
 __global__ void __launch_bounds__(kEThreads, 1)
 k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
            const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ CUtensorMap tm_wl,
            const float *__restrict__ bias, const float *__restrict__ c32,
-           const double *__restrict__ c64, float *__restrict__ R, double *__restrict__ part,
-           int64_t n, int K, int *err) {
+           const double *__restrict__ c64, float *__restrict__ lsc, __half *__restrict__ Rh,
+           __half *__restrict__ Rl, int64_t np, double *__restrict__ part, int64_t n, int K, int *err) {
   extern __shared__ uint8_t smem_raw[];
   ESmem &S = *reinterpret_cast<ESmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -179,6 +230,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+    float *my_l = lsc + (size_t)blockIdx.x * K * kTileM + row;   // l_ij of this point, stride 128
     uint32_t ai = 0;
     double lsum = 0.0;
     bool ok = true;
@@ -222,7 +274,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         for (int q = 0; q < kCompPerGroup; q++) {
           const int j = g * kCompPerGroup + q;
           const float l = __ldg(c32 + j) - 0.5f * s[q];
-          if (valid) R[(size_t)j * n + i] = l;
+          my_l[(size_t)j * kTileM] = l;
           if (l > mx) {
             se = se * __expf(mx - l) + 1.f;
             mx = l;
@@ -238,8 +290,10 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         const float lse = mx + __logf(se);
         lsum += __ldg(c64 + jmax) - 0.5 * (double)smax + (double)__logf(se);
         for (int j = 0; j < K; j++) {
-          float *p = R + (size_t)j * n + i;
-          *p = __expf(*p - lse);
+          const float r = __expf(my_l[(size_t)j * kTileM] - lse);
+          const __half h = __float2half_rn(r);
+          Rh[(size_t)j * np + i] = h;
+          Rl[(size_t)j * np + i] = __float2half_rn(r - __half2float(h));
         }
       }
     }
@@ -254,6 +308,336 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
   __syncthreads();
   tc_fence_after();
   if (warp == 1) tmem_dealloc(tbase, 512);
+}
+
+// =============================================================== means
+// Per 64-point block: D[128 comps x 80] += Rh Bh^T + Rh Bl^T + Rl Bh^T with
+// B rows 0..63 = X^T (hi / lo) and row 64 of Bh = 1 (gives sum_i r_ij).
+// Four epilogue warps flush the FP32 accumulator to FP64 partials every
+// kFlushBlocks blocks (double-buffered TMEM, 2 x 128 columns).
+__global__ void __launch_bounds__(192, 1)
+k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CUtensorMap tm_rl,
+           const __grid_constant__ CUtensorMap tm_xht, const __grid_constant__ CUtensorMap tm_xlt,
+           int64_t n, double *__restrict__ part, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  MSmem &S = *reinterpret_cast<MSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nblocks = (n + kBlk - 1) / kBlk;
+  // blocks of this CTA: b = blockIdx.x + t * gridDim.x, t < mine
+  const int64_t mine = nblocks > blockIdx.x ? (nblocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int64_t nwin = (mine + kFlushBlocks - 1) / kFlushBlocks;
+
+  // constant rows 64..79 of the B tiles (row 64 of Bh = ones; the rest zero);
+  // rows of 128 bytes, 16-byte chunk c of row r stored at c ^ (r & 7)
+  for (int e = threadIdx.x; e < 2 * 16 * kBlk; e += blockDim.x) {
+    const int s = e / (16 * kBlk), rem = e - s * 16 * kBlk;
+    const int r = 64 + rem / kBlk, col = rem % kBlk;   // logical (row, point)
+    const int phys = r * kBlk + (((col >> 3) ^ (r & 7)) << 3) + (col & 7);
+    S.bh[s][phys] = __float2half(r == 64 ? 1.f : 0.f);
+    S.bl[s][phys] = __float2half(0.f);
+  }
+  fence_proxy_async_smem();
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; s++) {
+      mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 1);
+      mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
+    }
+    mbar_init(&S.mma_done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(&S.tmem_base, 256);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem_base;
+  constexpr uint32_t kInBytes = 2 * kMaxK * kBlk * 2 + 2 * kD * kBlk * 2;
+
+  if (warp == 0) {
+    if (elect_one()) {
+      bool ok = true;
+      for (int64_t t = 0; t < mine && ok; t++) {
+        const int s = t & 1;
+        if (!(ok = mbar_wait(&S.in_empty[s], ((t >> 1) & 1) ^ 1, err))) break;
+        const int p0 = (int)((blockIdx.x + t * gridDim.x) * kBlk);
+        mbar_expect_tx(&S.in_full[s], kInBytes);
+        tma_load_2d(S.rh[s], &tm_rh, &S.in_full[s], p0, 0);
+        tma_load_2d(S.rl[s], &tm_rl, &S.in_full[s], p0, 0);
+        tma_load_2d(S.bh[s], &tm_xht, &S.in_full[s], p0, 0);
+        tma_load_2d(S.bl[s], &tm_xlt, &S.in_full[s], p0, 0);
+      }
+      for (int64_t u = mine - 1; u >= 0 && u >= mine - 2; u--)
+        mbar_wait_drain(&S.in_full[u & 1], (u >> 1) & 1);
+    }
+  } else if (warp == 1) {
+    if (elect_one()) {
+      bool ok = true;
+      for (int64_t w = 0; w < nwin && ok; w++) {
+        const int ab = w & 1;
+        if (!(ok = mbar_wait(&S.acc_empty[ab], ((w >> 1) & 1) ^ 1, err))) break;
+        const int64_t t1 = std::min<int64_t>(mine, (w + 1) * kFlushBlocks);
+        for (int64_t t = w * kFlushBlocks; t < t1; t++) {
+          const int s = t & 1;
+          if (!(ok = mbar_wait(&S.in_full[s], (t >> 1) & 1, err))) break;
+          tc_fence_after();
+          const uint64_t drh = sdesc_sw128(smem_u32(S.rh[s])), drl = sdesc_sw128(smem_u32(S.rl[s]));
+          const uint64_t dbh = sdesc_sw128(smem_u32(S.bh[s])), dbl = sdesc_sw128(smem_u32(S.bl[s]));
+#pragma unroll
+          for (int p = 0; p < 3; p++) {
+            const uint64_t da = (p == 2) ? drl : drh;
+            const uint64_t db = (p == 1) ? dbl : dbh;
+#pragma unroll
+            for (int kb = 0; kb < kBlk / 16; kb++)
+              mma_f16(tbase + ab * 128, da + 2 * kb, db + 2 * kb, idesc_f16(128, kMeanN),
+                      (t != w * kFlushBlocks) || p || kb);
+          }
+          mma_commit(&S.in_empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&S.acc_full[ab]);
+      }
+      mma_commit(&S.mma_done);
+      mbar_wait_drain(&S.mma_done, 0);
+    }
+  } else {
+    // flush: lane row = component; 80 columns -> FP64 partial
+    const int quad = warp & 3;
+    const int comp = quad * 32 + lane;
+    double *o = part + ((size_t)blockIdx.x * kMaxK + comp) * kMeanN;   // this CTA's FP64 partial
+    for (int c = 0; c < kMeanN; c++) o[c] = 0.0;
+    bool ok = true;
+    for (int64_t w = 0; w < nwin && ok; w++) {
+      const int ab = w & 1;
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (w >> 1) & 1, err)))) break;
+      tc_fence_after();
+      const uint32_t ta = tbase + ((uint32_t)(quad * 32) << 16) + ab * 128;
+#pragma unroll 1
+      for (int c0 = 0; c0 < 96; c0 += 32) {   // columns 80..95 are not used
+        uint32_t v[32];
+        tmem_ld32(ta + c0, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 32; c++)
+          if (c0 + c < kMeanN) o[c0 + c] += (double)__uint_as_float(v[c]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tbase, 256);
+}
+
+// S1 = sum r, mu = S2 / S1, pi = S1 / N (FP64, blocks summed in order)
+__global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, int64_t n,
+                                 double *__restrict__ mu, double *__restrict__ pi,
+                                 double *__restrict__ psum, float *__restrict__ muf) {
+  const int j = blockIdx.x;
+  __shared__ double s1;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += part[((size_t)g * kMaxK + j) * kMeanN + kD];
+    s1 = s;
+    psum[j] = s;
+    pi[j] = s / (double)n;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < kD; q += blockDim.x) {
+    double s = 0.0;
+    for (int g = 0; g < G; g++) s += part[((size_t)g * kMaxK + j) * kMeanN + q];
+    const double m = s / s1;
+    mu[(size_t)j * kD + q] = m;
+    muf[(size_t)j * kD + q] = (float)m;
+  }
+}
+
+// ========================================================= covariances
+// CTA (blockIdx.x = group of 4 components, blockIdx.y = chunk of points).
+// Producer thread t (warps 2..9): component q = t / 64 of the group, dim
+// a = t % 64; it writes row (q % 2) * 64 + a of pair q / 2's operand tile
+// (8 points per 16-byte store, 128-byte swizzle) and sums z^2 exactly.
+__global__ void __launch_bounds__(kCThreads, 1)
+k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUtensorMap tm_rh4,
+         const __grid_constant__ CUtensorMap tm_rl4, const float *__restrict__ muf, int64_t n,
+         int64_t blocks_per_chunk, double *__restrict__ cpart, double *__restrict__ dpart, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  CSmem &S = *reinterpret_cast<CSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int grp = blockIdx.x;
+  const int64_t nblocks = (n + kBlk - 1) / kBlk;
+  const int64_t b0 = (int64_t)blockIdx.y * blocks_per_chunk;
+  const int64_t mine = std::max<int64_t>(0, std::min<int64_t>(nblocks, b0 + blocks_per_chunk) - b0);
+  const int64_t nwin = (mine + kFlushBlocks - 1) / kFlushBlocks;
+  const size_t cta = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; s++) {
+      mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 8);
+      mbar_init(&S.z_full[s], 8), mbar_init(&S.z_empty[s], 1);
+      mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
+    }
+    mbar_init(&S.mma_done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(&S.tmem_base, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem_base;
+  constexpr uint32_t kInBytes = kBlk * kD * 4 + 2 * 4 * kBlk * 2;
+
+  if (warp == 0) {
+    if (elect_one()) {
+      bool ok = true;
+      for (int64_t t = 0; t < mine && ok; t++) {
+        const int s = t & 1;
+        if (!(ok = mbar_wait(&S.in_empty[s], ((t >> 1) & 1) ^ 1, err))) break;
+        const int p0 = (int)((b0 + t) * kBlk);
+        mbar_expect_tx(&S.in_full[s], kInBytes);
+        tma_load_2d(S.xs[s], &tm_x32, &S.in_full[s], 0, p0);
+        tma_load_2d(S.rh[s], &tm_rh4, &S.in_full[s], p0, grp * 4);
+        tma_load_2d(S.rl[s], &tm_rl4, &S.in_full[s], p0, grp * 4);
+      }
+      for (int64_t u = mine - 1; u >= 0 && u >= mine - 2; u--)
+        mbar_wait_drain(&S.in_full[u & 1], (u >> 1) & 1);
+    }
+  } else if (warp == 1) {
+    if (elect_one()) {
+      bool ok = true;
+      constexpr uint32_t idesc = idesc_f16(128, 128);
+      for (int64_t w = 0; w < nwin && ok; w++) {
+        const int ab = w & 1;
+        if (!(ok = mbar_wait(&S.acc_empty[ab], ((w >> 1) & 1) ^ 1, err))) break;
+        const int64_t t1 = std::min<int64_t>(mine, (w + 1) * kFlushBlocks);
+        for (int64_t t = w * kFlushBlocks; t < t1; t++) {
+          const int s = t & 1;
+          if (!(ok = mbar_wait(&S.z_full[s], (t >> 1) & 1, err))) break;
+          tc_fence_after();
+#pragma unroll
+          for (int pr = 0; pr < 2; pr++) {
+            const uint64_t dz = sdesc_sw128(smem_u32(S.z[s][pr]));
+#pragma unroll
+            for (int kb = 0; kb < kBlk / 16; kb++)
+              mma_f16(tbase + ab * 256 + pr * 128, dz + 2 * kb, dz + 2 * kb, idesc,
+                      (t != w * kFlushBlocks) || kb);
+          }
+          mma_commit(&S.z_empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&S.acc_full[ab]);
+      }
+      mma_commit(&S.mma_done);
+      mbar_wait_drain(&S.mma_done, 0);
+    }
+  } else if (warp < 10) {
+    // ------------------------------------------------ producers
+    const int t = threadIdx.x - 64;             // 0..255
+    const int q = t >> 6, a = t & 63;
+    const int pr = q >> 1, row = ((q & 1) << 6) + a;
+    const float mu_a = muf[(size_t)(grp * 4 + q) * kD + a];
+    double diag = 0.0;
+    float dwin = 0.f;
+    bool ok = true;
+    for (int64_t tb = 0; tb < mine && ok; tb++) {
+      const int s = tb & 1;
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.in_full[s], (tb >> 1) & 1, err)))) break;
+      // sqrt(r) of (component t / 64, point t % 64), r = rh + rl
+      S.sr[s][t] = sqrtf(__half2float(S.rh[s][t]) + __half2float(S.rl[s][t]));
+      asm volatile("bar.sync 2, 256;" ::: "memory");
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.z_empty[s], ((tb >> 1) & 1) ^ 1, err)))) break;
+      const float *xr = S.xs[s];
+      const float *sq = S.sr[s] + q * kBlk;
+      uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[s][pr]) + row * 128;
+      const int64_t pbase = (b0 + tb) * kBlk;
+#pragma unroll
+      for (int c8 = 0; c8 < kBlk / 8; c8++) {
+        uint32_t w4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int p = c8 * 8 + 2 * u;
+          // rows past N are zero-filled in xs and r; keep them exactly zero
+          const float z0 = (pbase + p < n) ? (xr[p * kD + a] - mu_a) * sq[p] : 0.f;
+          const float z1 = (pbase + p + 1 < n) ? (xr[(p + 1) * kD + a] - mu_a) * sq[p + 1] : 0.f;
+          dwin = fmaf(z0, z0, dwin);
+          dwin = fmaf(z1, z1, dwin);
+          const __half2 hz = __floats2half2_rn(z0, z1);
+          w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+        }
+        *reinterpret_cast<uint4 *>(zrow + (((c8 ^ (row & 7)) & 7) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&S.z_full[s]);
+        mbar_arrive(&S.in_empty[s]);
+      }
+      if ((tb + 1) % kFlushBlocks == 0) {
+        diag += (double)dwin;
+        dwin = 0.f;
+      }
+    }
+    diag += (double)dwin;
+    dpart[(cta * 4 + q) * kD + a] = diag;
+  } else {
+    // ------------------------------------------------ flush warps 10..13
+    const int quad = warp & 3;
+    const int lrow = quad * 32 + lane;          // TMEM lane = row of the pair tile
+    const int half = lrow >> 6;                 // 0: first component of the pair, 1: second
+    double *o[2];                               // this CTA's FP64 partial rows
+#pragma unroll
+    for (int pr = 0; pr < 2; pr++) {
+      o[pr] = cpart + ((cta * 4 + pr * 2 + half) * kD + (lrow & 63)) * kD;
+      for (int c = 0; c < kD; c++) o[pr][c] = 0.0;
+    }
+    bool ok = true;
+    for (int64_t w = 0; w < nwin && ok; w++) {
+      const int ab = w & 1;
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (w >> 1) & 1, err)))) break;
+      tc_fence_after();
+#pragma unroll 1
+      for (int pc = 0; pc < 4; pc++) {          // (pair, 32-column chunk)
+        const int pr = pc >> 1, c0 = (pc & 1) * 32;
+        uint32_t v[32];
+        tmem_ld32(tbase + ((uint32_t)(quad * 32) << 16) + ab * 256 + pr * 128 + half * 64 + c0, v);
+        tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < 32; c++) o[pr][c0 + c] += (double)__uint_as_float(v[c]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tbase, 512);
+}
+
+// Covs_j = sym(S3_j) / S1_j with the exact diagonal (FP64, chunks in order)
+__global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *__restrict__ dpart, int gx,
+                               int gy, const double *__restrict__ psum, double *__restrict__ sigma) {
+  const int j = blockIdx.x, grp = j / 4, q = j % 4;
+  const double inv = 1.0 / psum[j];
+  double *Sg = sigma + (size_t)j * kD * kD;
+  for (int e = threadIdx.x; e < kD * kD; e += blockDim.x) {
+    const int a = e / kD, b = e - a * kD;
+    if (b < a) continue;
+    double s = 0.0;
+    if (a == b) {
+      for (int c = 0; c < gy; c++) s += dpart[(((size_t)c * gx + grp) * 4 + q) * kD + a];
+    } else {
+      for (int c = 0; c < gy; c++) {
+        const double *P = cpart + (((size_t)c * gx + grp) * 4 + q) * kD * kD;
+        s += 0.5 * (P[a * kD + b] + P[b * kD + a]);
+      }
+    }
+    s *= inv;
+    Sg[a * kD + b] = s;
+    Sg[b * kD + a] = s;
+  }
 }
 
 // ================================================ operand preparation
@@ -278,17 +662,37 @@ __global__ void k_prep_w(const double *__restrict__ linv, const double *__restri
   }
 }
 
-// x -> xh = fp16(x), xl = fp16(x - xh)
-__global__ void k_split_x(const float *__restrict__ X, int64_t count, __half *__restrict__ Xh,
-                          __half *__restrict__ Xl, float *__restrict__ amax) {
+// x -> xh = fp16(x), xl = fp16(x - xh), row-major and transposed (d x np)
+__global__ void k_split_x(const float *__restrict__ X, int64_t n, __half *__restrict__ Xh,
+                          __half *__restrict__ Xl, __half *__restrict__ XhT, __half *__restrict__ XlT,
+                          int64_t np, float *__restrict__ amax) {
+  __shared__ __half th[kD][65], tl[kD][65];
   float m = 0.f;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const float x = X[e];
-    const __half h = __float2half_rn(x);
-    Xh[e] = h;
-    Xl[e] = __float2half_rn(x - __half2float(h));
-    m = fmaxf(m, fabsf(x));
+  const int64_t nt = (n + 63) / 64;
+  for (int64_t tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+    const int64_t r0 = tile * 64;
+    for (int e = threadIdx.x; e < 64 * kD; e += blockDim.x) {
+      const int r = e / kD, c = e - r * kD;
+      if (r0 + r < n) {
+        const float x = X[(r0 + r) * kD + c];
+        const __half h = __float2half_rn(x);
+        const __half l = __float2half_rn(x - __half2float(h));
+        Xh[(r0 + r) * kD + c] = h;
+        Xl[(r0 + r) * kD + c] = l;
+        th[c][r] = h;
+        tl[c][r] = l;
+        m = fmaxf(m, fabsf(x));
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * kD; e += blockDim.x) {
+      const int c = e / 64, r = e - c * 64;
+      if (r0 + r < n) {
+        XhT[(size_t)c * np + r0 + r] = th[c][r];
+        XlT[(size_t)c * np + r0 + r] = tl[c][r];
+      }
+    }
+    __syncthreads();
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
@@ -305,44 +709,103 @@ __global__ void k_reduce_parts(const double *__restrict__ part, int np, DevStatu
   }
 }
 
-// ==================================================== host: tensor maps
-static int encode_2d(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint32_t box_cols,
-                     uint32_t box_rows) {
-  return encode_tmap_2d(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, cols, rows, box_cols, box_rows,
-                        CU_TENSOR_MAP_SWIZZLE_128B);
+__global__ void k_flag_timeout(DevStatus *st, const int *__restrict__ err) {
+  if (threadIdx.x == 0 && *err) st->timeout = 1;
 }
 
-static size_t esmem_bytes() { return sizeof(ESmem) + 1024; }
+// posteriors (hi + lo) -> n x K double rows
+__global__ void k_post_rows_tc(const __half *__restrict__ Rh, const __half *__restrict__ Rl, int64_t np,
+                               int K, int64_t r0, int64_t rows, double *__restrict__ out) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= rows * K) return;
+  const int64_t i = e / K;
+  const int j = (int)(e - i * K);
+  const size_t o = (size_t)j * np + r0 + i;
+  out[e] = (double)__half2float(Rh[o]) + (double)__half2float(Rl[o]);
+}
 
-bool em_tc_supported(int d, int k) { return d == kD && k % kCompPerGroup == 0 && k <= 1024; }
+__global__ void k_classes_tc(const __half *__restrict__ Rh, const __half *__restrict__ Rl, int64_t np,
+                             int64_t n, int K, int32_t *__restrict__ cls) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float best = -1.f;
+  int bj = -1;
+  for (int j = 0; j < K; j++) {
+    const float v = __half2float(Rh[(size_t)j * np + i]) + __half2float(Rl[(size_t)j * np + i]);
+    if (v > best) {
+      best = v;
+      bj = j;
+    }
+  }
+  cls[i] = bj;
+}
+
+// ============================================================== host side
+static size_t esmem_bytes() { return sizeof(ESmem) + 1024; }
+static size_t msmem_bytes() { return sizeof(MSmem) + 1024; }
+static size_t csmem_bytes() { return sizeof(CSmem) + 1024; }
+
+static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint64_t pitch_elems,
+                    uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz) {
+  return encode_tmap_2d(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, cols, rows, box_cols, box_rows, swz,
+                        pitch_elems * 2);
+}
+
+bool em_tc_supported(int d, int k) { return d == kD && k % kCompPerGroup == 0 && k <= kMaxK; }
 
 int em_tc_create(fem_em *h) {
   TcEmPlan *p = new TcEmPlan();
   h->tc = p;
   const int K = h->k;
   const int64_t n = h->n;
+  p->np = (n + 63) / 64 * 64;
+  const int sms = sm_count();
   FEM_TRY(dalloc(&h->Xhi, (size_t)n * kD));
   FEM_TRY(dalloc(&h->Xlo, (size_t)n * kD));
+  FEM_TRY(dalloc(&p->XhT, (size_t)kD * p->np));
+  FEM_TRY(dalloc(&p->XlT, (size_t)kD * p->np));
+  FEM_TRY(dalloc(&p->Rh, (size_t)K * p->np));
+  FEM_TRY(dalloc(&p->Rl, (size_t)K * p->np));
   FEM_TRY(dalloc(&p->Wh, (size_t)K * kD * kD));
   FEM_TRY(dalloc(&p->Wl, (size_t)K * kD * kD));
   FEM_TRY(dalloc(&p->bias, (size_t)K * kD));
+  FEM_TRY(dalloc(&p->muf, (size_t)K * kD));
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
-  p->egrid = (int)std::min<int64_t>(sm_count(), (n + kTileM - 1) / kTileM);
+  p->egrid = (int)std::min<int64_t>(sms, (n + kTileM - 1) / kTileM);
   FEM_TRY(dalloc(&p->epart, p->egrid));
-  FEM_TRY(encode_2d(&p->tm_xh, h->Xhi, kD, (uint64_t)n, kD, kTileM));
-  FEM_TRY(encode_2d(&p->tm_xl, h->Xlo, kD, (uint64_t)n, kD, kTileM));
-  FEM_TRY(encode_2d(&p->tm_wh, p->Wh, kD, (uint64_t)K * kD, kD, kGroupN));
-  FEM_TRY(encode_2d(&p->tm_wl, p->Wl, kD, (uint64_t)K * kD, kD, kGroupN));
+  FEM_TRY(dalloc(&p->lsc, (size_t)p->egrid * K * kTileM));
+  const int64_t nblocks = (n + kBlk - 1) / kBlk;
+  p->mgrid = (int)std::min<int64_t>(sms, nblocks);
+  FEM_TRY(dalloc(&p->mpart, (size_t)p->mgrid * kMaxK * kMeanN));
+  p->cgx = K / 4;
+  p->cgy = (int)std::max<int64_t>(1, std::min<int64_t>(nblocks, (4 * sms + p->cgx - 1) / p->cgx));
+  FEM_TRY(dalloc(&p->cpart, (size_t)p->cgx * p->cgy * 4 * kD * kD));
+  FEM_TRY(dalloc(&p->dpart, (size_t)p->cgx * p->cgy * 4 * kD));
+  // E-step operands
+  FEM_TRY(fp16_map(&p->tm_xh, h->Xhi, kD, n, kD, kD, kTileM, CU_TENSOR_MAP_SWIZZLE_128B));
+  FEM_TRY(fp16_map(&p->tm_xl, h->Xlo, kD, n, kD, kD, kTileM, CU_TENSOR_MAP_SWIZZLE_128B));
+  FEM_TRY(fp16_map(&p->tm_wh, p->Wh, kD, (uint64_t)K * kD, kD, kD, kGroupN, CU_TENSOR_MAP_SWIZZLE_128B));
+  FEM_TRY(fp16_map(&p->tm_wl, p->Wl, kD, (uint64_t)K * kD, kD, kD, kGroupN, CU_TENSOR_MAP_SWIZZLE_128B));
+  // means operands: rows of np-pitched component-major / transposed arrays
+  FEM_TRY(encode_tmap_2d(&p->tm_rh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rh, (uint64_t)n, (uint64_t)K, kBlk,
+                         kMaxK, CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
+  FEM_TRY(encode_tmap_2d(&p->tm_rl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rl, (uint64_t)n, (uint64_t)K, kBlk,
+                         kMaxK, CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
+  FEM_TRY(encode_tmap_2d(&p->tm_xht, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->XhT, (uint64_t)n, kD, kBlk, kD,
+                         CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
+  FEM_TRY(encode_tmap_2d(&p->tm_xlt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->XlT, (uint64_t)n, kD, kBlk, kD,
+                         CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
+  // covariance operands (no swizzle: read by CUDA cores)
+  FEM_TRY(encode_tmap_2d(&p->tm_x32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->X, kD, (uint64_t)n, kD, kBlk,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, 0));
+  FEM_TRY(encode_tmap_2d(&p->tm_rh4, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rh, (uint64_t)n, (uint64_t)K, kBlk, 4,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, (uint64_t)p->np * 2));
+  FEM_TRY(encode_tmap_2d(&p->tm_rl4, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rl, (uint64_t)n, (uint64_t)K, kBlk, 4,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, (uint64_t)p->np * 2));
   FEM_CUDA(cudaFuncSetAttribute(k_estep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem_bytes()));
-  // the M-step runs on the FP32 CUDA-core kernels
-  h->mgrid = (int)std::min<int64_t>((int64_t)4 * sm_count(), (n + 31) / 32);
-  FEM_TRY(dalloc(&h->mpart, (size_t)h->mgrid * K * (kD + 1)));
-  int TB, nb, nblk;
-  cov_geometry(kD, &TB, &nb, &nblk);
-  const int gx = (K * nblk + 255) / 256;
-  h->cchunks = (int)std::max<int64_t>(1, std::min<int64_t>((3 * sm_count() + gx - 1) / gx, (n + 31) / 32));
-  FEM_TRY(dalloc(&h->cpart, (size_t)h->cchunks * K * nblk * TB * TB));
+  FEM_CUDA(cudaFuncSetAttribute(k_means_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem_bytes()));
+  FEM_CUDA(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem_bytes()));
   return FEM_OK;
 }
 
@@ -352,19 +815,28 @@ void em_tc_destroy(fem_em *h) {
   dfree(p->Wh);
   dfree(p->Wl);
   dfree(p->bias);
+  dfree(p->Rh);
+  dfree(p->Rl);
+  dfree(p->XhT);
+  dfree(p->XlT);
+  dfree(p->lsc);
   dfree(p->epart);
+  dfree(p->mpart);
+  dfree(p->cpart);
+  dfree(p->dpart);
+  dfree(p->muf);
   dfree(p->err);
   delete p;
   h->tc = nullptr;
 }
 
 int em_tc_upload(fem_em *h) {
+  TcEmPlan *p = h->tc;
   float *amax = nullptr;
   FEM_TRY(dalloc(&amax, 1));
   FEM_CUDA(cudaMemsetAsync(amax, 0, sizeof(float), h->stream));
-  const int64_t count = h->n * kD;
-  const int blocks = (int)std::min<int64_t>(4096, (count + 255) / 256);
-  k_split_x<<<blocks, 256, 0, h->stream>>>(h->X, count, h->Xhi, h->Xlo, amax);
+  const int blocks = (int)std::min<int64_t>(4 * sm_count(), (h->n + 63) / 64);
+  k_split_x<<<blocks, 256, 0, h->stream>>>(h->X, h->n, h->Xhi, h->Xlo, p->XhT, p->XlT, p->np, amax);
   float m = 0.f;
   cudaMemcpyAsync(&m, amax, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
@@ -391,8 +863,8 @@ int em_tc_prepare(fem_em *h) {
 int em_tc_estep(fem_em *h) {
   TcEmPlan *p = h->tc;
   k_estep_tc<<<p->egrid, kEThreads, esmem_bytes(), h->stream>>>(
-      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, (const float *)h->logcT, h->logc, (float *)h->R,
-      p->epart, h->n, h->k, p->err);
+      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, (const float *)h->logcT, h->logc, p->lsc, p->Rh, p->Rl,
+      p->np, p->epart, h->n, h->k, p->err);
   FEM_CUDA(cudaGetLastError());
   k_reduce_parts<<<1, 32, 0, h->stream>>>(p->epart, p->egrid, h->dstat, p->err);
   FEM_CUDA(cudaGetLastError());
@@ -400,6 +872,39 @@ int em_tc_estep(fem_em *h) {
   return FEM_OK;
 }
 
-int em_tc_mstep(fem_em *h) { return em_plain_mstep(h); }
+int em_tc_mstep(fem_em *h) {
+  TcEmPlan *p = h->tc;
+  const int K = h->k;
+  k_means_tc<<<p->mgrid, 192, msmem_bytes(), h->stream>>>(p->tm_rh, p->tm_rl, p->tm_xht, p->tm_xlt, h->n,
+                                                           p->mpart, p->err);
+  FEM_CUDA(cudaGetLastError());
+  k_final_means_tc<<<K, 64, 0, h->stream>>>(p->mpart, p->mgrid, K, h->n, h->mu, h->pi, h->psum, p->muf);
+  FEM_CUDA(cudaGetLastError());
+  const int64_t nblocks = (h->n + kBlk - 1) / kBlk;
+  const int64_t bpc = (nblocks + p->cgy - 1) / p->cgy;
+  k_cov_tc<<<dim3(p->cgx, p->cgy), kCThreads, csmem_bytes(), h->stream>>>(p->tm_x32, p->tm_rh4, p->tm_rl4, p->muf,
+                                                                         h->n, bpc, p->cpart, p->dpart, p->err);
+  FEM_CUDA(cudaGetLastError());
+  k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->psum, h->sigma);
+  FEM_CUDA(cudaGetLastError());
+  k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
+  h->launches += 5;
+  return FEM_OK;
+}
+
+int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout) {
+  TcEmPlan *p = h->tc;
+  const int64_t tot = rows * h->k;
+  k_post_rows_tc<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(p->Rh, p->Rl, p->np, h->k, r0, rows, dout);
+  FEM_CUDA(cudaGetLastError());
+  return FEM_OK;
+}
+
+int em_tc_classes(fem_em *h, int32_t *dcls) {
+  TcEmPlan *p = h->tc;
+  k_classes_tc<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(p->Rh, p->Rl, p->np, h->n, h->k, dcls);
+  FEM_CUDA(cudaGetLastError());
+  return FEM_OK;
+}
 
 }  // namespace fem

@@ -35,9 +35,11 @@ void set_error(const char *fmt, ...);
 // Checks that `device` exists and is an sm_103 part; selects it.
 int select_device(int device);
 
-// 2-D row-major tensor map (cols contiguous), resolved without linking libcuda
+// 2-D row-major tensor map (cols contiguous, rows pitch_bytes apart; 0 =
+// packed), resolved without linking libcuda
 int encode_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, const void *base, uint64_t cols,
-                   uint64_t rows, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz);
+                   uint64_t rows, uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz,
+                   uint64_t pitch_bytes = 0);
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the live count)
 int sm_count();

@@ -34,6 +34,30 @@ def test_tc_estep_matches_oracle(gpu_lib, oracle, n, k):
     assert np.abs(post - post_o).max() <= 1e-4
 
 
+@pytest.mark.parametrize("n,k", [(1 << 15, 16), (3000 + 5, 128)])
+def test_tc_mstep_matches_oracle(gpu_lib, oracle, n, k):
+    """M-step alone: the oracle's M-step applied to the GPU's posteriors."""
+    X, init, _, _ = estep_case(oracle, n, k)
+    with CudaMatrixEM(64, n, k, precision="mixed") as em:
+        em.CopyDataset(X)
+        em.SetMixture(GaussianMixture(*init))
+        em.InitDensities()
+        em.PrecomputeDensityMatrix()
+        post = em.Posteriors()
+        em.MStep()
+        G = em.GetMixture()
+    pi, mu, sg = oracle.mstep(X, post)
+    np.testing.assert_allclose(G.weights, pi, rtol=1e-6, atol=1e-12)
+    scale = np.sqrt(np.einsum("jaa->ja", sg))
+    assert np.max(np.abs(G.means - mu) / scale) <= 1e-5
+    rel = np.abs(G.covs - sg) / (scale[:, :, None] * scale[:, None, :])
+    print("mixed M-step max |dmu|/sigma = %.2e, max |dSigma|/(s_a s_b) = %.2e"
+          % (np.max(np.abs(G.means - mu) / scale), rel.max()))
+    assert rel.max() <= 1e-3
+    diag = np.abs(np.einsum("jaa->ja", G.covs) / np.einsum("jaa->ja", sg) - 1)
+    assert diag.max() <= 1e-5
+
+
 def test_tc_sweeps_em_large_shape(gpu_lib, oracle):
     """em_large shape (d=64) at N=2^17, K=32: 8 sweeps, per-sweep logL."""
     n, k = 1 << 17, 32
