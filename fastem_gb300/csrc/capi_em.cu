@@ -384,8 +384,10 @@ int fem_em_train(fem_em *h, int svd, double *logl_trace, double *e_trace, int ca
     }
   }
   int it;
+  if (h->timing) FEM_CUDA(cudaEventRecord(h->ev[6], h->stream));
   for (it = 1; it <= h->cfg.max_sweeps; it++) {
     FEM_TRY(reset_status(h));
+    if (h->timing) h->sweeps++;
     FEM_TRY(enqueue_estep(h));
     FEM_TRY(enqueue_mstep(h));
     FEM_TRY(enqueue_factor(h));
@@ -413,6 +415,14 @@ int fem_em_train(fem_em *h, int svd, double *logl_trace, double *e_trace, int ca
       it++;
       break;
     }
+  }
+  if (h->timing) {
+    // ev[6] .. ev[7] brackets every sweep of this loop (host waits included)
+    FEM_CUDA(cudaEventRecord(h->ev[7], h->stream));
+    FEM_CUDA(cudaEventSynchronize(h->ev[7]));
+    float ms = 0.f;
+    FEM_CUDA(cudaEventElapsedTime(&ms, h->ev[6], h->ev[7]));
+    h->t_train += ms;
   }
   if (iter_counter) *iter_counter = it;
   if (logl_out) *logl_out = logl;
@@ -485,8 +495,15 @@ int fem_em_get_factors(fem_em *h, double *U, double *logdet) {
 int fem_em_timing_reset(fem_em *h, int enable) {
   FEM_TRY(check_handle(h));
   h->timing = enable != 0;
-  h->t_estep = h->t_mstep = h->t_final = 0.0;
-  h->launches = 0;
+  h->t_estep = h->t_mstep = h->t_final = h->t_train = 0.0;
+  h->launches = h->sweeps = 0;
+  return FEM_OK;
+}
+
+int fem_em_timing_total(fem_em *h, double *train_ms, int64_t *sweeps) {
+  FEM_TRY(check_handle(h));
+  if (train_ms) *train_ms = h->t_train;
+  if (sweeps) *sweeps = h->sweeps;
   return FEM_OK;
 }
 

@@ -105,6 +105,7 @@ struct TcEmPlan {
   CUtensorMap tm_x32, tm_rh4, tm_rl4;          // covariances
   __half *Wh = nullptr, *Wl = nullptr;  // (K*d) x d, permuted rows
   float *bias = nullptr;                // K*d, permuted
+  float *clo = nullptr;                 // log coefficient - float(log coefficient)
   __half *Rh = nullptr, *Rl = nullptr;  // K x np posteriors hi / lo
   __half *XhT = nullptr, *XlT = nullptr;  // d x np
   int64_t np = 0;                       // padded row pitch (multiple of 64)
@@ -126,7 +127,7 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 __global__ void __launch_bounds__(kEThreads, 1)
 k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
            const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ CUtensorMap tm_wl,
-           const float *__restrict__ bias, const float *__restrict__ c32,
+           const float *__restrict__ bias, const float *__restrict__ chi, const float *__restrict__ clo,
            const double *__restrict__ c64, float *__restrict__ lsc, __half *__restrict__ Rh,
            __half *__restrict__ Rl, int64_t np, double *__restrict__ part, int64_t n, int K, int *err) {
   extern __shared__ uint8_t smem_raw[];
@@ -273,7 +274,9 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
 #pragma unroll
         for (int q = 0; q < kCompPerGroup; q++) {
           const int j = g * kCompPerGroup + q;
-          const float l = __ldg(c32 + j) - 0.5f * s[q];
+          // c_j carried as float hi + lo: its rounding would shift every
+          // posterior of component j by the same factor
+          const float l = (__ldg(chi + j) - 0.5f * s[q]) + __ldg(clo + j);
           my_l[(size_t)j * kTileM] = l;
           if (l > mx) {
             se = se * __expf(mx - l) + 1.f;
@@ -290,7 +293,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         const float lse = mx + __logf(se);
         lsum += __ldg(c64 + jmax) - 0.5 * (double)smax + (double)__logf(se);
         for (int j = 0; j < K; j++) {
-          const float r = __expf(my_l[(size_t)j * kTileM] - lse);
+          const float r = expf(my_l[(size_t)j * kTileM] - lse);
           const __half h = __float2half_rn(r);
           Rh[(size_t)j * np + i] = h;
           Rl[(size_t)j * np + i] = __float2half_rn(r - __half2float(h));
@@ -643,8 +646,10 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
 // ================================================ operand preparation
 // W = L^-1 (FP64) -> FP16 hi/lo in the permuted row order; b = L^-1 mu
 __global__ void k_prep_w(const double *__restrict__ linv, const double *__restrict__ mu, int K,
-                         __half *__restrict__ Wh, __half *__restrict__ Wl, float *__restrict__ bias) {
+                         __half *__restrict__ Wh, __half *__restrict__ Wl, float *__restrict__ bias,
+                         const double *__restrict__ logc, float *__restrict__ clo) {
   const int j = blockIdx.x;
+  if (threadIdx.x == 0) clo[j] = (float)(logc[j] - (double)(float)logc[j]);
   const int g = j / kCompPerGroup, q = j % kCompPerGroup;
   for (int e = threadIdx.x; e < kD * kD; e += blockDim.x) {
     const int k = e / kD, m = e - k * kD;
@@ -769,6 +774,7 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(dalloc(&p->Wh, (size_t)K * kD * kD));
   FEM_TRY(dalloc(&p->Wl, (size_t)K * kD * kD));
   FEM_TRY(dalloc(&p->bias, (size_t)K * kD));
+  FEM_TRY(dalloc(&p->clo, K));
   FEM_TRY(dalloc(&p->muf, (size_t)K * kD));
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
@@ -815,6 +821,7 @@ void em_tc_destroy(fem_em *h) {
   dfree(p->Wh);
   dfree(p->Wl);
   dfree(p->bias);
+  dfree(p->clo);
   dfree(p->Rh);
   dfree(p->Rl);
   dfree(p->XhT);
@@ -854,7 +861,7 @@ int em_tc_upload(fem_em *h) {
 
 int em_tc_prepare(fem_em *h) {
   TcEmPlan *p = h->tc;
-  k_prep_w<<<h->k, 256, 0, h->stream>>>(h->linv, h->mu, h->k, p->Wh, p->Wl, p->bias);
+  k_prep_w<<<h->k, 256, 0, h->stream>>>(h->linv, h->mu, h->k, p->Wh, p->Wl, p->bias, h->logc, p->clo);
   FEM_CUDA(cudaGetLastError());
   h->launches += 1;
   return FEM_OK;
@@ -863,7 +870,7 @@ int em_tc_prepare(fem_em *h) {
 int em_tc_estep(fem_em *h) {
   TcEmPlan *p = h->tc;
   k_estep_tc<<<p->egrid, kEThreads, esmem_bytes(), h->stream>>>(
-      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, (const float *)h->logcT, h->logc, p->lsc, p->Rh, p->Rl,
+      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, (const float *)h->logcT, p->clo, h->logc, p->lsc, p->Rh, p->Rl,
       p->np, p->epart, h->n, h->k, p->err);
   FEM_CUDA(cudaGetLastError());
   k_reduce_parts<<<1, 32, 0, h->stream>>>(p->epart, p->egrid, h->dstat, p->err);

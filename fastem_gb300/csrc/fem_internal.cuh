@@ -126,8 +126,8 @@ struct fem_em {
   bool timing = false;
   unsigned tmask = 0;            // event slots recorded since the last sync
   cudaEvent_t ev[8] = {};
-  double t_estep = 0, t_mstep = 0, t_final = 0;
-  int64_t launches = 0;
+  double t_estep = 0, t_mstep = 0, t_final = 0, t_train = 0;
+  int64_t launches = 0, sweeps = 0;
 };
 
 struct fem_km {

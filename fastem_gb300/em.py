@@ -186,4 +186,7 @@ class CudaMatrixEM:
         n = ctypes.c_int64()
         C.check(C.lib().fem_em_timing_get(self._h, ctypes.byref(e), ctypes.byref(m),
                                           ctypes.byref(f), ctypes.byref(n)))
-        return dict(estep_ms=e.value, mstep_ms=m.value, factor_ms=f.value, launches=n.value)
+        t, sw = ctypes.c_double(), ctypes.c_int64()
+        C.check(C.lib().fem_em_timing_total(self._h, ctypes.byref(t), ctypes.byref(sw)))
+        return dict(estep_ms=e.value, mstep_ms=m.value, factor_ms=f.value, launches=n.value,
+                    train_ms=t.value, sweeps=sw.value)

@@ -132,6 +132,9 @@ int fem_em_get_factors(fem_em *h, double *U, double *logdet);
 int fem_em_timing_reset(fem_em *h, int enable);
 int fem_em_timing_get(fem_em *h, double *estep_ms, double *mstep_ms, double *finalize_ms,
                       int64_t *launches);
+/* device time (ms) from the first to the last kernel of every
+ * fem_em_train sweep loop since the last reset, and the sweeps it ran */
+int fem_em_timing_total(fem_em *h, double *train_ms, int64_t *sweeps);
 
 /* ============================== k-means ============================== */
 
