@@ -5,20 +5,23 @@
 // finalisers:
 //
 //  1. E-step (MatrixEMBase::BlockDensities + PostProcessDensityMatrix,
-//     EM2/MatrixEM.cpp:39-51,69-81): ONE GEMM of each 128-point tile against
-//     the stacked inverse Cholesky factors of all components,
+//     EM2/MatrixEM.cpp:39-51,69-81): ONE GEMM of the points against the
+//     stacked inverse Cholesky factors of all components,
 //       Y = X W^T,  W = [L_1^-1; ...; L_K^-1],  y_jk = (L_j^-1 x)_k,
 //     in FP16 x 3 (x = xh + xl, W = Wh + Wl: Xh Wh^T + Xh Wl^T + Xl Wh^T)
-//     with FP32 accumulation in TMEM.  The epilogue subtracts b_j = L_j^-1
-//     mu_j, squares and sums each component's 64 columns, adds the log
-//     coefficient and keeps an online log-sum-exp per point; the
-//     posteriors r_ij = exp(l_ij - LSE_i) are stored as FP16 hi/lo pairs
-//     (component-major).  The per-point log-likelihood is summed in FP64
-//     with the FP64 log coefficient of the winning component.
-//     Within a group of 4 components the 256 accumulator columns are
-//     ordered by 16-wide k-block, highest first, so K-step kb only needs
-//     the first 256-64kb columns (L^-1 is lower triangular): 37.5% of the
-//     MMA work is skipped.
+//     with FP32 accumulation in TMEM.  A CTA works on a pair of 128-point
+//     tiles so every W group fetched from L2 feeds two M=128 MMAs.  The
+//     epilogue subtracts b_j = L_j^-1 mu_j (kept in shared memory), squares
+//     and sums each component's 64 columns, adds the log coefficient (float
+//     hi + lo) and keeps an online log-sum-exp per point; the posteriors
+//     r_ij = exp(l_ij - LSE_i) of the previous pair are finished while the
+//     current pair's groups drain, and stored as FP16 hi/lo pairs
+//     (component-major).  The per-point log-likelihood is summed in FP64 with
+//     the FP64 log coefficient of the winning component.
+//     Within a group of 2 components the 128 accumulator columns are ordered
+//     by 16-wide k-block, highest first, so K-step kb only needs the first
+//     128-32kb columns (L^-1 is lower triangular): 37.5% of the MMA work is
+//     skipped.
 //  2. Means (doMStep means part, EM2/MatrixEM.cpp:319-343): S2 = R^T X and
 //     S1 = R^T 1 as one GEMM per 64-point block, A = [Rh | Rl] (components
 //     x points), B = [Xh^T; 1] / [Xl^T; 0] (80 rows x points); FP32 in TMEM,
@@ -52,23 +55,27 @@ using namespace tc;
 
 // ------------------------------------------------------------ constants
 constexpr int kD = 64;                   // dimension handled by the tensor-core path
-constexpr int kTileM = 128;              // E-step points per tile
-constexpr int kGroupN = 256;             // E-step accumulator columns per component group
+constexpr int kTileM = 128;              // E-step points per tile (two tiles per CTA step)
+constexpr int kGroupN = 128;             // E-step accumulator columns per component group
 constexpr int kCompPerGroup = kGroupN / kD;
-constexpr int kXStages = 2, kWStages = 2;
+constexpr int kWStages = 4;
 constexpr uint32_t kXBytes = kTileM * kD * 2;    // one FP16 X tile (16 KB)
-constexpr uint32_t kWBytes = kGroupN * kD * 2;   // one FP16 W group (32 KB)
+constexpr uint32_t kWBytes = kGroupN * kD * 2;   // one FP16 W group (16 KB)
 constexpr int kEThreads = 192;
 constexpr int kBlk = 64;                 // M-step points per block (one 128-byte swizzle row)
 constexpr int kFlushBlocks = 64;         // FP32 TMEM window: 64 blocks = 4096 points
 constexpr int kMaxK = 128;               // components handled by one means M-tile
+constexpr int kMStages = 3;              // means input ring
+constexpr int kCIn = 6;                  // covariance input ring
 
 struct __align__(1024) ESmem {
-  __half xh[kXStages][kTileM * kD];
-  __half xl[kXStages][kTileM * kD];
+  __half xh[2][kTileM * kD];   // the two tiles of the current pair
+  __half xl[2][kTileM * kD];
   __half wh[kWStages][kGroupN * kD];
   __half wl[kWStages][kGroupN * kD];
-  uint64_t x_full[kXStages], x_empty[kXStages];
+  float bias[kMaxK * kD];      // b = L^-1 mu, permuted like the accumulator columns
+  float chi[kMaxK], clo[kMaxK];
+  uint64_t x_full, x_empty;
   uint64_t w_full[kWStages], w_empty[kWStages];
   uint64_t acc_full[2], acc_empty[2];
   uint64_t mma_done;
@@ -79,22 +86,22 @@ struct __align__(1024) ESmem {
 // means kernel: A = Rh/Rl (128 comps x 64 points), B = [X^T; 1] (80 x 64)
 constexpr int kMeanN = 80;
 struct __align__(1024) MSmem {
-  __half rh[2][kMaxK * kBlk];
-  __half rl[2][kMaxK * kBlk];
-  __half bh[2][kMeanN * kBlk];   // rows 0..63 X_h^T, row 64 ones, rows 65..79 zero
-  __half bl[2][kMeanN * kBlk];   // rows 0..63 X_l^T, rows 64..79 zero
-  uint64_t in_full[2], in_empty[2], acc_full[2], acc_empty[2], mma_done;
+  __half rh[kMStages][kMaxK * kBlk];
+  __half rl[kMStages][kMaxK * kBlk];
+  __half bh[kMStages][kMeanN * kBlk];   // rows 0..63 X_h^T, row 64 ones, rows 65..79 zero
+  __half bl[kMStages][kMeanN * kBlk];   // rows 0..63 X_l^T, rows 64..79 zero
+  uint64_t in_full[kMStages], in_empty[kMStages], acc_full[2], acc_empty[2], mma_done;
   uint32_t tmem_base;
 };
 
 // covariance kernel: 4 components per CTA (2 pairs), 64-point blocks
 struct __align__(1024) CSmem {
   __half z[2][2][128 * kBlk];    // [stage][pair] 128 rows (comp q dims) x 64 points, SW128
-  float xs[2][kBlk * kD];        // X tile (points x dims)
-  __half rh[2][4 * kBlk];
-  __half rl[2][4 * kBlk];
+  float xs[kCIn][kBlk * kD];     // X tile (points x dims)
+  __half rh[kCIn][4 * kBlk];
+  __half rl[kCIn][4 * kBlk];
   float sr[2][4 * kBlk];         // sqrt(r)
-  uint64_t in_full[2], in_empty[2], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
+  uint64_t in_full[kCIn], in_empty[kCIn], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
   uint32_t tmem_base;
 };
 constexpr int kCThreads = 448;   // warp 0 TMA, 1 MMA, 2..9 producers, 10..13 flush
@@ -109,7 +116,7 @@ struct TcEmPlan {
   __half *Rh = nullptr, *Rl = nullptr;  // K x np posteriors hi / lo
   __half *XhT = nullptr, *XlT = nullptr;  // d x np
   int64_t np = 0;                       // padded row pitch (multiple of 64)
-  float *lsc = nullptr;                 // E-step scratch: egrid x K x 128
+  float *lsc = nullptr;                 // E-step scratch: egrid x 2 x K x 256
   double *epart = nullptr;              // per-CTA log-likelihood
   double *mpart = nullptr;              // means partials: mgrid x 128 x 80
   double *cpart = nullptr;              // covariance partials: cgrid x 4 x 64 x 64
@@ -121,6 +128,12 @@ struct TcEmPlan {
 
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void store_post(__half *Rh, __half *Rl, size_t o, float r) {
+  const __half h = __float2half_rn(r);
+  Rh[o] = h;
+  Rl[o] = __float2half_rn(r - __half2float(h));
 }
 
 // ============================================================== E-step
@@ -135,9 +148,12 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = K / kCompPerGroup;
   const int64_t ntiles = (n + kTileM - 1) / kTileM;
+  const int64_t npairs = (ntiles + 1) / 2;
 
+  for (int e = threadIdx.x; e < K * kD; e += blockDim.x) S.bias[e] = bias[e];
+  for (int j = threadIdx.x; j < K; j += blockDim.x) S.chi[j] = chi[j], S.clo[j] = clo[j];
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kXStages; s++) mbar_init(&S.x_full[s], 1), mbar_init(&S.x_empty[s], 1);
+    mbar_init(&S.x_full, 1), mbar_init(&S.x_empty, 1);
     for (int s = 0; s < kWStages; s++) mbar_init(&S.w_full[s], 1), mbar_init(&S.w_empty[s], 1);
     for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
     mbar_init(&S.mma_done, 1);
@@ -158,12 +174,16 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
       tma_prefetch_desc(&tm_wl);
       uint32_t xi = 0, wi = 0;
       bool ok = true;
-      for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int xs = xi % kXStages;
-        if (!(ok = mbar_wait(&S.x_empty[xs], ((xi / kXStages) & 1) ^ 1, err))) break;
-        mbar_expect_tx(&S.x_full[xs], 2 * kXBytes);
-        tma_load_2d(S.xh[xs], &tm_xh, &S.x_full[xs], 0, (int)(tile * kTileM));
-        tma_load_2d(S.xl[xs], &tm_xl, &S.x_full[xs], 0, (int)(tile * kTileM));
+      for (int64_t pr = blockIdx.x; pr < npairs && ok; pr += gridDim.x) {
+        if (!(ok = mbar_wait(&S.x_empty, (xi & 1) ^ 1, err))) break;
+        const bool has1 = 2 * pr + 1 < ntiles;
+        mbar_expect_tx(&S.x_full, (has1 ? 4 : 2) * kXBytes);
+        tma_load_2d(S.xh[0], &tm_xh, &S.x_full, 0, (int)(2 * pr * kTileM));
+        tma_load_2d(S.xl[0], &tm_xl, &S.x_full, 0, (int)(2 * pr * kTileM));
+        if (has1) {
+          tma_load_2d(S.xh[1], &tm_xh, &S.x_full, 0, (int)((2 * pr + 1) * kTileM));
+          tma_load_2d(S.xl[1], &tm_xl, &S.x_full, 0, (int)((2 * pr + 1) * kTileM));
+        }
         xi++;
         for (int g = 0; g < G; g++) {
           const int ws = wi % kWStages;
@@ -175,10 +195,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         }
       }
       // drain: the last loads must land before the CTA may exit
-      for (int s = 0; s < kXStages && xi > (uint32_t)s; s++) {
-        const uint32_t u = xi - 1 - s;
-        mbar_wait_drain(&S.x_full[u % kXStages], (u / kXStages) & 1);
-      }
+      if (xi > 0) mbar_wait_drain(&S.x_full, (xi - 1) & 1);
       for (int s = 0; s < kWStages && wi > (uint32_t)s; s++) {
         const uint32_t u = wi - 1 - s;
         mbar_wait_drain(&S.w_full[u % kWStages], (u / kWStages) & 1);
@@ -189,12 +206,15 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
     if (elect_one()) {
       uint32_t xi = 0, wi = 0, ai = 0;
       bool ok = true;
-      for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int xs = xi % kXStages;
-        if (!(ok = mbar_wait(&S.x_full[xs], (xi / kXStages) & 1, err))) break;
+      for (int64_t pr = blockIdx.x; pr < npairs && ok; pr += gridDim.x) {
+        if (!(ok = mbar_wait(&S.x_full, xi & 1, err))) break;
         tc_fence_after();
-        const uint64_t dxh = sdesc_sw128(smem_u32(S.xh[xs]));
-        const uint64_t dxl = sdesc_sw128(smem_u32(S.xl[xs]));
+        const int nt = (2 * pr + 1 < ntiles) ? 2 : 1;
+        uint64_t dxh[2], dxl[2];
+        for (int t = 0; t < 2; t++) {
+          dxh[t] = sdesc_sw128(smem_u32(S.xh[t]));
+          dxl[t] = sdesc_sw128(smem_u32(S.xl[t]));
+        }
         for (int g = 0; g < G; g++) {
           const int ws = wi % kWStages, ab = ai & 1;
           if (!(ok = mbar_wait(&S.acc_empty[ab], ((ai >> 1) & 1) ^ 1, err))) break;
@@ -202,16 +222,17 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
           tc_fence_after();
           const uint64_t dwh = sdesc_sw128(smem_u32(S.wh[ws]));
           const uint64_t dwl = sdesc_sw128(smem_u32(S.wl[ws]));
-          const uint32_t dt = tbase + ab * kGroupN;
+          for (int t = 0; t < nt; t++) {
+            const uint32_t dt = tbase + (2 * ab + t) * kGroupN;
 #pragma unroll
-          for (int p = 0; p < 3; p++) {
-            const uint64_t da = (p == 2) ? dxl : dxh;
-            const uint64_t db = (p == 1) ? dwl : dwh;
+            for (int p = 0; p < 3; p++) {
+              const uint64_t da = (p == 2) ? dxl[t] : dxh[t];
+              const uint64_t db = (p == 1) ? dwl : dwh;
 #pragma unroll
-            for (int kb = 0; kb < kD / 16; kb++) {
-              // +32 bytes per 16-element K step inside the 128-byte swizzle row
-              mma_f16(dt, da + 2 * kb, db + 2 * kb, idesc_f16(kTileM, kGroupN - 64 * kb),
-                      (p | kb) != 0);
+              for (int kb = 0; kb < kD / 16; kb++) {
+                // +32 bytes per 16-element K step inside the 128-byte swizzle row
+                mma_f16(dt, da + 2 * kb, db + 2 * kb, idesc_f16(kTileM, kGroupN - 32 * kb), (p | kb) != 0);
+              }
             }
           }
           mma_commit(&S.w_empty[ws]);
@@ -219,7 +240,8 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
           wi++;
           ai++;
         }
-        mma_commit(&S.x_empty[xs]);
+        if (!ok) break;
+        mma_commit(&S.x_empty);
         xi++;
       }
       // every MMA issued must complete before TMEM is released
@@ -231,72 +253,118 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
-    float *my_l = lsc + (size_t)blockIdx.x * K * kTileM + row;   // l_ij of this point, stride 128
-    uint32_t ai = 0;
+    // l_ij scratch of this CTA: [pair parity][component][256 points of the pair]
+    float *scr = lsc + (size_t)blockIdx.x * 2 * K * (2 * kTileM);
     double lsum = 0.0;
     bool ok = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-      const int64_t i = tile * kTileM + row;
-      const bool valid = i < n;
-      float mx = -INFINITY, se = 0.f, smax = 0.f;
-      int jmax = 0;
+    bool have_prev = false;
+    int prev_par = 0;
+    int64_t prev_i[2] = {-1, -1};
+    float prev_lse[2] = {0.f, 0.f};
+    uint32_t ai = 0;
+    int pc = 0;
+    for (int64_t pr = blockIdx.x; pr < npairs && ok; pr += gridDim.x, pc++) {
+      const int par = pc & 1;
+      const int nt = (2 * pr + 1 < ntiles) ? 2 : 1;
+      int64_t pi[2];
+      float mx[2] = {-INFINITY, -INFINITY}, se[2] = {0.f, 0.f}, smax[2] = {0.f, 0.f};
+      int jmax[2] = {0, 0};
+      for (int t = 0; t < 2; t++) pi[t] = (t < nt && (2 * pr + t) * kTileM + row < n) ? (2 * pr + t) * kTileM + row : -1;
       for (int g = 0; g < G; g++) {
+        // posteriors of components 2g, 2g+1 of the previous pair: load early
+        float lp[2][2];
+        if (have_prev) {
+#pragma unroll
+          for (int t = 0; t < 2; t++)
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+              lp[t][q] = scr[((size_t)(prev_par * K + 2 * g + q)) * (2 * kTileM) + t * kTileM + row];
+        }
         const int ab = ai & 1;
         // warp-uniform outcome: the TMEM loads below are .sync.aligned
         if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (ai >> 1) & 1, err)))) break;
         tc_fence_after();
-        float s[kCompPerGroup] = {0.f, 0.f, 0.f, 0.f};
-        const float *bg = bias + (size_t)g * kGroupN;
-        // 64-column block bp holds k-block (3 - bp) of all 4 components:
-        // column 64 bp + 16 q + t belongs to component q
+        float s[2][kCompPerGroup] = {{0.f, 0.f}, {0.f, 0.f}};
+        const float *bg = S.bias + g * kGroupN;
+        // 32-column block bp holds k-block (3 - bp) of both components:
+        // column 32 bp + 16 q + t belongs to component q
 #pragma unroll 1
-        for (int bp = 0; bp < kGroupN / 64; bp++) {
+        for (int bp = 0; bp < kGroupN / 32; bp++) {
           uint32_t v[2][32];
-          tmem_ld32(tbase + lane_addr + ab * kGroupN + bp * 64, v[0]);
-          tmem_ld32(tbase + lane_addr + ab * kGroupN + bp * 64 + 32, v[1]);
-          const float4 *b4 = reinterpret_cast<const float4 *>(bg + bp * 64);
-          float4 b[16];
+          tmem_ld32(tbase + lane_addr + (2 * ab) * kGroupN + bp * 32, v[0]);
+          if (nt > 1) tmem_ld32(tbase + lane_addr + (2 * ab + 1) * kGroupN + bp * 32, v[1]);
+          float4 b[8];
+          const float4 *b4 = reinterpret_cast<const float4 *>(bg + bp * 32);
 #pragma unroll
-          for (int t = 0; t < 16; t++) b[t] = __ldg(b4 + t);
+          for (int u = 0; u < 8; u++) b[u] = b4[u];
           tmem_wait_ld();
 #pragma unroll
-          for (int t = 0; t < 64; t++) {
+          for (int t = 0; t < 32; t++) {
             const float bb = (t & 3) == 0 ? b[t >> 2].x : (t & 3) == 1 ? b[t >> 2].y
                            : (t & 3) == 2 ? b[t >> 2].z : b[t >> 2].w;
-            const float y = __uint_as_float(v[t >> 5][t & 31]) - bb;
-            s[t >> 4] = fmaf(y, y, s[t >> 4]);
+            const float y0 = __uint_as_float(v[0][t]) - bb;
+            s[0][t >> 4] = fmaf(y0, y0, s[0][t >> 4]);
+            if (nt > 1) {
+              const float y1 = __uint_as_float(v[1][t]) - bb;
+              s[1][t >> 4] = fmaf(y1, y1, s[1][t >> 4]);
+            }
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
         ai++;
+        if (have_prev) {
 #pragma unroll
-        for (int q = 0; q < kCompPerGroup; q++) {
-          const int j = g * kCompPerGroup + q;
-          // c_j carried as float hi + lo: its rounding would shift every
-          // posterior of component j by the same factor
-          const float l = (__ldg(chi + j) - 0.5f * s[q]) + __ldg(clo + j);
-          my_l[(size_t)j * kTileM] = l;
-          if (l > mx) {
-            se = se * __expf(mx - l) + 1.f;
-            mx = l;
-            jmax = j;
-            smax = s[q];
-          } else if (l > -INFINITY) {
-            se += __expf(l - mx);
+          for (int t = 0; t < 2; t++)
+            if (prev_i[t] >= 0)
+#pragma unroll
+              for (int q = 0; q < 2; q++)
+                store_post(Rh, Rl, (size_t)(2 * g + q) * np + prev_i[t], expf(lp[t][q] - prev_lse[t]));
+        }
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+#pragma unroll
+          for (int q = 0; q < kCompPerGroup; q++) {
+            const int j = g * kCompPerGroup + q;
+            // c_j carried as float hi + lo: its rounding would shift every
+            // posterior of component j by the same factor
+            const float l = (S.chi[j] - 0.5f * s[t][q]) + S.clo[j];
+            scr[((size_t)(par * K + j)) * (2 * kTileM) + t * kTileM + row] = l;
+            if (l > mx[t]) {
+              se[t] = se[t] * __expf(mx[t] - l) + 1.f;
+              mx[t] = l;
+              jmax[t] = j;
+              smax[t] = s[t][q];
+            } else if (l > -INFINITY) {
+              se[t] += __expf(l - mx[t]);
+            }
           }
         }
       }
       if (!ok) break;
-      if (valid) {
-        const float lse = mx + __logf(se);
-        lsum += __ldg(c64 + jmax) - 0.5 * (double)smax + (double)__logf(se);
-        for (int j = 0; j < K; j++) {
-          const float r = expf(my_l[(size_t)j * kTileM] - lse);
-          const __half h = __float2half_rn(r);
-          Rh[(size_t)j * np + i] = h;
-          Rl[(size_t)j * np + i] = __float2half_rn(r - __half2float(h));
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        prev_i[t] = pi[t];
+        prev_lse[t] = mx[t] + __logf(se[t]);
+        if (pi[t] >= 0) lsum += c64[jmax[t]] - 0.5 * (double)smax[t] + (double)__logf(se[t]);
+      }
+      prev_par = par;
+      have_prev = true;
+    }
+    // posteriors of the last pair
+    if (ok && have_prev) {
+#pragma unroll
+      for (int t = 0; t < 2; t++) {
+        if (prev_i[t] < 0) continue;
+        for (int j0 = 0; j0 < K; j0 += 8) {
+          float l8[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++)
+            l8[u] = (j0 + u < K) ? scr[((size_t)(prev_par * K + j0 + u)) * (2 * kTileM) + t * kTileM + row] : 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; u++)
+            if (j0 + u < K) store_post(Rh, Rl, (size_t)(j0 + u) * np + prev_i[t], expf(l8[u] - prev_lse[t]));
         }
       }
     }
@@ -332,7 +400,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
 
   // constant rows 64..79 of the B tiles (row 64 of Bh = ones; the rest zero);
   // rows of 128 bytes, 16-byte chunk c of row r stored at c ^ (r & 7)
-  for (int e = threadIdx.x; e < 2 * 16 * kBlk; e += blockDim.x) {
+  for (int e = threadIdx.x; e < kMStages * 16 * kBlk; e += blockDim.x) {
     const int s = e / (16 * kBlk), rem = e - s * 16 * kBlk;
     const int r = 64 + rem / kBlk, col = rem % kBlk;   // logical (row, point)
     const int phys = r * kBlk + (((col >> 3) ^ (r & 7)) << 3) + (col & 7);
@@ -341,10 +409,8 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
   }
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
-    for (int s = 0; s < 2; s++) {
-      mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 1);
-      mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
-    }
+    for (int s = 0; s < kMStages; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 1);
+    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
   }
@@ -359,8 +425,8 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
     if (elect_one()) {
       bool ok = true;
       for (int64_t t = 0; t < mine && ok; t++) {
-        const int s = t & 1;
-        if (!(ok = mbar_wait(&S.in_empty[s], ((t >> 1) & 1) ^ 1, err))) break;
+        const int s = (int)(t % kMStages);
+        if (!(ok = mbar_wait(&S.in_empty[s], ((t / kMStages) & 1) ^ 1, err))) break;
         const int p0 = (int)((blockIdx.x + t * gridDim.x) * kBlk);
         mbar_expect_tx(&S.in_full[s], kInBytes);
         tma_load_2d(S.rh[s], &tm_rh, &S.in_full[s], p0, 0);
@@ -368,8 +434,8 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
         tma_load_2d(S.bh[s], &tm_xht, &S.in_full[s], p0, 0);
         tma_load_2d(S.bl[s], &tm_xlt, &S.in_full[s], p0, 0);
       }
-      for (int64_t u = mine - 1; u >= 0 && u >= mine - 2; u--)
-        mbar_wait_drain(&S.in_full[u & 1], (u >> 1) & 1);
+      for (int64_t u = mine - 1; u >= 0 && u >= mine - kMStages; u--)
+        mbar_wait_drain(&S.in_full[u % kMStages], (u / kMStages) & 1);
     }
   } else if (warp == 1) {
     if (elect_one()) {
@@ -379,8 +445,8 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
         if (!(ok = mbar_wait(&S.acc_empty[ab], ((w >> 1) & 1) ^ 1, err))) break;
         const int64_t t1 = std::min<int64_t>(mine, (w + 1) * kFlushBlocks);
         for (int64_t t = w * kFlushBlocks; t < t1; t++) {
-          const int s = t & 1;
-          if (!(ok = mbar_wait(&S.in_full[s], (t >> 1) & 1, err))) break;
+          const int s = (int)(t % kMStages);
+          if (!(ok = mbar_wait(&S.in_full[s], (t / kMStages) & 1, err))) break;
           tc_fence_after();
           const uint64_t drh = sdesc_sw128(smem_u32(S.rh[s])), drl = sdesc_sw128(smem_u32(S.rl[s]));
           const uint64_t dbh = sdesc_sw128(smem_u32(S.bh[s])), dbl = sdesc_sw128(smem_u32(S.bl[s]));
@@ -476,8 +542,8 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
   const size_t cta = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
 
   if (threadIdx.x == 0) {
+    for (int s = 0; s < kCIn; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 8);
     for (int s = 0; s < 2; s++) {
-      mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 8);
       mbar_init(&S.z_full[s], 8), mbar_init(&S.z_empty[s], 1);
       mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
     }
@@ -495,16 +561,16 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     if (elect_one()) {
       bool ok = true;
       for (int64_t t = 0; t < mine && ok; t++) {
-        const int s = t & 1;
-        if (!(ok = mbar_wait(&S.in_empty[s], ((t >> 1) & 1) ^ 1, err))) break;
+        const int s = (int)(t % kCIn);
+        if (!(ok = mbar_wait(&S.in_empty[s], ((t / kCIn) & 1) ^ 1, err))) break;
         const int p0 = (int)((b0 + t) * kBlk);
         mbar_expect_tx(&S.in_full[s], kInBytes);
         tma_load_2d(S.xs[s], &tm_x32, &S.in_full[s], 0, p0);
         tma_load_2d(S.rh[s], &tm_rh4, &S.in_full[s], p0, grp * 4);
         tma_load_2d(S.rl[s], &tm_rl4, &S.in_full[s], p0, grp * 4);
       }
-      for (int64_t u = mine - 1; u >= 0 && u >= mine - 2; u--)
-        mbar_wait_drain(&S.in_full[u & 1], (u >> 1) & 1);
+      for (int64_t u = mine - 1; u >= 0 && u >= mine - kCIn; u--)
+        mbar_wait_drain(&S.in_full[u % kCIn], (u / kCIn) & 1);
     }
   } else if (warp == 1) {
     if (elect_one()) {
@@ -544,37 +610,40 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     float dwin = 0.f;
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
-      const int s = tb & 1;
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.in_full[s], (tb >> 1) & 1, err)))) break;
+      const int si = (int)(tb % kCIn), sz = tb & 1;
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.in_full[si], (tb / kCIn) & 1, err)))) break;
       // sqrt(r) of (component t / 64, point t % 64), r = rh + rl
-      S.sr[s][t] = sqrtf(__half2float(S.rh[s][t]) + __half2float(S.rl[s][t]));
+      S.sr[sz][t] = sqrtf(__half2float(S.rh[si][t]) + __half2float(S.rl[si][t]));
       asm volatile("bar.sync 2, 256;" ::: "memory");
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.z_empty[s], ((tb >> 1) & 1) ^ 1, err)))) break;
-      const float *xr = S.xs[s];
-      const float *sq = S.sr[s] + q * kBlk;
-      uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[s][pr]) + row * 128;
+      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err)))) break;
+      const float *xr = S.xs[si];
+      const float *sq = S.sr[sz] + q * kBlk;
+      uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][pr]) + row * 128;
       const int64_t pbase = (b0 + tb) * kBlk;
 #pragma unroll
       for (int c8 = 0; c8 < kBlk / 8; c8++) {
         uint32_t w4[4];
+        const float4 sa = *reinterpret_cast<const float4 *>(sq + c8 * 8);
+        const float4 sb = *reinterpret_cast<const float4 *>(sq + c8 * 8 + 4);
+        const float sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           const int p = c8 * 8 + 2 * u;
           // rows past N are zero-filled in xs and r; keep them exactly zero
-          const float z0 = (pbase + p < n) ? (xr[p * kD + a] - mu_a) * sq[p] : 0.f;
-          const float z1 = (pbase + p + 1 < n) ? (xr[(p + 1) * kD + a] - mu_a) * sq[p + 1] : 0.f;
+          const float z0 = (pbase + p < n) ? (xr[p * kD + a] - mu_a) * sv[2 * u] : 0.f;
+          const float z1 = (pbase + p + 1 < n) ? (xr[(p + 1) * kD + a] - mu_a) * sv[2 * u + 1] : 0.f;
           dwin = fmaf(z0, z0, dwin);
           dwin = fmaf(z1, z1, dwin);
           const __half2 hz = __floats2half2_rn(z0, z1);
           w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
         }
-        *reinterpret_cast<uint4 *>(zrow + (((c8 ^ (row & 7)) & 7) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
       }
       fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) {
-        mbar_arrive(&S.z_full[s]);
-        mbar_arrive(&S.in_empty[s]);
+        mbar_arrive(&S.z_full[sz]);
+        mbar_arrive(&S.in_empty[si]);
       }
       if ((tb + 1) % kFlushBlocks == 0) {
         diag += (double)dwin;
@@ -644,16 +713,22 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
 }
 
 // ================================================ operand preparation
-// W = L^-1 (FP64) -> FP16 hi/lo in the permuted row order; b = L^-1 mu
+// W = L^-1 (FP64) -> FP16 hi/lo in the permuted row order; b = L^-1 mu;
+// row of (component j, output k) = group j/2, k-block position 3 - k/16,
+// component j%2, k%16
+__device__ __forceinline__ int w_row(int j, int k) {
+  return (j / kCompPerGroup) * kGroupN + (kD / 16 - 1 - k / 16) * (16 * kCompPerGroup) +
+         (j % kCompPerGroup) * 16 + (k & 15);
+}
+
 __global__ void k_prep_w(const double *__restrict__ linv, const double *__restrict__ mu, int K,
                          __half *__restrict__ Wh, __half *__restrict__ Wl, float *__restrict__ bias,
                          const double *__restrict__ logc, float *__restrict__ clo) {
   const int j = blockIdx.x;
   if (threadIdx.x == 0) clo[j] = (float)(logc[j] - (double)(float)logc[j]);
-  const int g = j / kCompPerGroup, q = j % kCompPerGroup;
   for (int e = threadIdx.x; e < kD * kD; e += blockDim.x) {
     const int k = e / kD, m = e - k * kD;
-    const int row = g * kGroupN + (kD / 16 - 1 - k / 16) * 64 + q * 16 + (k & 15);
+    const int row = w_row(j, k);
     const double w = linv[(size_t)j * kD * kD + e];
     const __half h = __double2half(w);
     Wh[(size_t)row * kD + m] = h;
@@ -662,8 +737,7 @@ __global__ void k_prep_w(const double *__restrict__ linv, const double *__restri
   for (int k = threadIdx.x; k < kD; k += blockDim.x) {
     double b = 0.0;
     for (int m = 0; m <= k; m++) b += linv[(size_t)j * kD * kD + k * kD + m] * mu[(size_t)j * kD + m];
-    const int row = g * kGroupN + (kD / 16 - 1 - k / 16) * 64 + q * 16 + (k & 15);
-    bias[row] = (float)b;
+    bias[w_row(j, k)] = (float)b;
   }
 }
 
@@ -756,7 +830,8 @@ static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t ro
                         pitch_elems * 2);
 }
 
-bool em_tc_supported(int d, int k) { return d == kD && k % kCompPerGroup == 0 && k <= kMaxK; }
+// the covariance kernel works on groups of 4 components
+bool em_tc_supported(int d, int k) { return d == kD && k % 4 == 0 && k <= kMaxK; }
 
 int em_tc_create(fem_em *h) {
   TcEmPlan *p = new TcEmPlan();
@@ -778,9 +853,10 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(dalloc(&p->muf, (size_t)K * kD));
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
-  p->egrid = (int)std::min<int64_t>(sms, (n + kTileM - 1) / kTileM);
+  const int64_t npairs = ((n + kTileM - 1) / kTileM + 1) / 2;
+  p->egrid = (int)std::min<int64_t>(sms, npairs);
   FEM_TRY(dalloc(&p->epart, p->egrid));
-  FEM_TRY(dalloc(&p->lsc, (size_t)p->egrid * K * kTileM));
+  FEM_TRY(dalloc(&p->lsc, (size_t)p->egrid * 2 * K * 2 * kTileM));
   const int64_t nblocks = (n + kBlk - 1) / kBlk;
   p->mgrid = (int)std::min<int64_t>(sms, nblocks);
   FEM_TRY(dalloc(&p->mpart, (size_t)p->mgrid * kMaxK * kMeanN));

@@ -63,6 +63,33 @@ def test_tc_mstep_matches_oracle(gpu_lib, oracle, n, k):
     assert diag.max() <= 1e-5
 
 
+def test_tc_steps_at_converged_params(gpu_lib, oracle):
+    """E-step and M-step evaluated at the oracle's parameters after 8 sweeps
+    (tight covariances), each against the oracle on the same inputs."""
+    n, k = 1 << 18, 16
+    X, _ = synth.em_large(seed=3, n=n, d=64, k=k)
+    init = synth.dsquared_init(X, k, seed=5)
+    ref = oracle.em_train(X, *init, 8, eps=0.0)
+    pi, mu, sg = ref["pi"], ref["mu"], ref["sigma"]
+    st, U, ld, _ = oracle.init_densities(sg)
+    post_o, ll_o = oracle.estep(X, pi, mu, U, ld)
+    with CudaMatrixEM(64, n, k, precision="mixed") as em:
+        em.CopyDataset(X)
+        em.SetMixture(GaussianMixture(pi, mu, sg))
+        em.InitDensities()
+        ll = em.PrecomputeDensityMatrix()
+        post = em.Posteriors()
+        em.MStep()
+        G = em.GetMixture()
+    pi2, mu2, sg2 = oracle.mstep(X, post)
+    scale = np.sqrt(np.einsum("jaa->ja", sg2))
+    print("converged: E-step |dlogL/N| = %.2e, sum r - 1 = %.2e, M-step |dpi/pi| %.2e, |dmu|/sigma %.2e, "
+          "|dSigma|/(s_a s_b) %.2e" % (abs(ll - ll_o) / n, post.sum(axis=1).mean() - 1,
+                                       np.max(np.abs(G.weights / pi2 - 1)), np.max(np.abs(G.means - mu2) / scale),
+                                       np.max(np.abs(G.covs - sg2) / (scale[:, :, None] * scale[:, None, :]))))
+    assert abs(ll - ll_o) / n <= 1e-6
+
+
 def run_sweeps(oracle, n, k, sweeps):
     X, _ = synth.em_large(seed=3, n=n, d=64, k=k)
     init = synth.dsquared_init(X, k, seed=5)
