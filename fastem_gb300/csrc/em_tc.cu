@@ -101,6 +101,7 @@ struct __align__(1024) CSmem {
   __half rh[kCIn][4 * kBlk];
   __half rl[kCIn][4 * kBlk];
   float sr[2][4 * kBlk];         // sqrt(r)
+  double dred[4][4][kD];         // exact-diagonal partials of the 4 point slices
   uint64_t in_full[kCIn], in_empty[kCIn], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
   uint32_t tmem_base;
 };
@@ -224,10 +225,13 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
           const uint64_t dwl = sdesc_sw128(smem_u32(S.wl[ws]));
           for (int t = 0; t < nt; t++) {
             const uint32_t dt = tbase + (2 * ab + t) * kGroupN;
+            // the small cross products Xh Wl and Xl Wh first, Xh Wh last: the
+            // accumulator is rounded after every MMA, and it only grows to
+            // |W x| during the final four steps
 #pragma unroll
             for (int p = 0; p < 3; p++) {
-              const uint64_t da = (p == 2) ? dxl[t] : dxh[t];
-              const uint64_t db = (p == 1) ? dwl : dwh;
+              const uint64_t da = (p == 1) ? dxl[t] : dxh[t];
+              const uint64_t db = (p == 0) ? dwl : dwh;
 #pragma unroll
               for (int kb = 0; kb < kD / 16; kb++) {
                 // +32 bytes per 16-element K step inside the 128-byte swizzle row
@@ -602,12 +606,15 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     }
   } else if (warp < 10) {
     // ------------------------------------------------ producers
+    // thread t: dimension a = t % 64 and the 16-point slice pc = t / 64 of
+    // the block, for all 4 components (x is read once per point)
     const int t = threadIdx.x - 64;             // 0..255
-    const int q = t >> 6, a = t & 63;
-    const int pr = q >> 1, row = ((q & 1) << 6) + a;
-    const float mu_a = muf[(size_t)(grp * 4 + q) * kD + a];
-    double diag = 0.0;
-    float dwin = 0.f;
+    const int a = t & 63, pc = t >> 6;
+    float mu_a[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) mu_a[q] = muf[(size_t)(grp * 4 + q) * kD + a];
+    double diag[4] = {0.0, 0.0, 0.0, 0.0};
+    float dwin[4] = {0.f, 0.f, 0.f, 0.f};
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
       const int si = (int)(tb % kCIn), sz = tb & 1;
@@ -617,27 +624,37 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
       asm volatile("bar.sync 2, 256;" ::: "memory");
       if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err)))) break;
       const float *xr = S.xs[si];
-      const float *sq = S.sr[sz] + q * kBlk;
-      uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][pr]) + row * 128;
       const int64_t pbase = (b0 + tb) * kBlk;
 #pragma unroll
-      for (int c8 = 0; c8 < kBlk / 8; c8++) {
-        uint32_t w4[4];
-        const float4 sa = *reinterpret_cast<const float4 *>(sq + c8 * 8);
-        const float4 sb = *reinterpret_cast<const float4 *>(sq + c8 * 8 + 4);
-        const float sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+      for (int h = 0; h < 2; h++) {             // two 8-point chunks of the slice
+        const int c8 = pc * 2 + h;
+        float xv[8];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int p = c8 * 8 + 2 * u;
+        for (int u = 0; u < 8; u++) {
+          const int p = c8 * 8 + u;
           // rows past N are zero-filled in xs and r; keep them exactly zero
-          const float z0 = (pbase + p < n) ? (xr[p * kD + a] - mu_a) * sv[2 * u] : 0.f;
-          const float z1 = (pbase + p + 1 < n) ? (xr[(p + 1) * kD + a] - mu_a) * sv[2 * u + 1] : 0.f;
-          dwin = fmaf(z0, z0, dwin);
-          dwin = fmaf(z1, z1, dwin);
-          const __half2 hz = __floats2half2_rn(z0, z1);
-          w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+          xv[u] = (pbase + p < n) ? xr[p * kD + a] : 0.f;
         }
-        *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const float *sq = S.sr[sz] + q * kBlk + c8 * 8;
+          const float4 sa = *reinterpret_cast<const float4 *>(sq);
+          const float4 sb = *reinterpret_cast<const float4 *>(sq + 4);
+          const float sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+          uint32_t w4[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const float z0 = (xv[2 * u] - mu_a[q]) * sv[2 * u];
+            const float z1 = (xv[2 * u + 1] - mu_a[q]) * sv[2 * u + 1];
+            dwin[q] = fmaf(z0, z0, dwin[q]);
+            dwin[q] = fmaf(z1, z1, dwin[q]);
+            const __half2 hz = __floats2half2_rn(z0, z1);
+            w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+          }
+          const int row = ((q & 1) << 6) + a;
+          uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
+          *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        }
       }
       fence_proxy_async_smem();
       __syncwarp();
@@ -646,12 +663,18 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         mbar_arrive(&S.in_empty[si]);
       }
       if ((tb + 1) % kFlushBlocks == 0) {
-        diag += (double)dwin;
-        dwin = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q], dwin[q] = 0.f;
       }
     }
-    diag += (double)dwin;
-    dpart[(cta * 4 + q) * kD + a] = diag;
+    // exact diagonal: combine the 4 point slices in a fixed order
+#pragma unroll
+    for (int q = 0; q < 4; q++) S.dred[pc][q][a] = diag[q] + (double)dwin[q];
+    asm volatile("bar.sync 2, 256;" ::: "memory");
+    if (pc == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        dpart[(cta * 4 + q) * kD + a] = ((S.dred[0][q][a] + S.dred[1][q][a]) + S.dred[2][q][a]) + S.dred[3][q][a];
   } else {
     // ------------------------------------------------ flush warps 10..13
     const int quad = warp & 3;
