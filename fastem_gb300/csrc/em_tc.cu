@@ -618,11 +618,12 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
       const int si = (int)(tb % kCIn), sz = tb & 1;
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.in_full[si], (tb / kCIn) & 1, err)))) break;
+      bool got = mbar_wait(&S.in_full[si], (tb / kCIn) & 1, err);
+      got = got && mbar_wait(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err);
       // sqrt(r) of (component t / 64, point t % 64), r = rh + rl
-      S.sr[sz][t] = sqrtf(__half2float(S.rh[si][t]) + __half2float(S.rl[si][t]));
-      asm volatile("bar.sync 2, 256;" ::: "memory");
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err)))) break;
+      if (got) S.sr[sz][t] = sqrtf(__half2float(S.rh[si][t]) + __half2float(S.rl[si][t]));
+      // one decision for all 256 producers (they meet at this barrier every block)
+      if (!(ok = bar_and(2, 256, got))) break;
       const float *xr = S.xs[si];
       const int64_t pbase = (b0 + tb) * kBlk;
 #pragma unroll
