@@ -61,7 +61,7 @@ constexpr int kCompPerGroup = kGroupN / kD;
 constexpr int kWStages = 4;
 constexpr uint32_t kXBytes = kTileM * kD * 2;    // one FP16 X tile (16 KB)
 constexpr uint32_t kWBytes = kGroupN * kD * 2;   // one FP16 W group (16 KB)
-constexpr int kEThreads = 192;
+constexpr int kEThreads = 320;  // warp 0 TMA, 1 MMA, 2..9 epilogue
 constexpr int kBlk = 64;                 // M-step points per block (one 128-byte swizzle row)
 constexpr int kFlushBlocks = 64;         // FP32 TMEM window: 64 blocks = 4096 points
 constexpr int kMaxK = 128;               // components handled by one means M-tile
@@ -80,7 +80,7 @@ struct __align__(1024) ESmem {
   uint64_t acc_full[2], acc_empty[2];
   uint64_t mma_done;
   uint32_t tmem_base;
-  double red[4];
+  double red[8];
 };
 
 // means kernel: A = Rh/Rl (128 comps x 64 points), B = [X^T; 1] (80 x 64)
@@ -156,7 +156,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
   if (threadIdx.x == 0) {
     mbar_init(&S.x_full, 1), mbar_init(&S.x_empty, 1);
     for (int s = 0; s < kWStages; s++) mbar_init(&S.w_full[s], 1), mbar_init(&S.w_empty[s], 1);
-    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
+    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 8);
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
   }
@@ -254,63 +254,58 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
     }
   } else {
     // ------------------------------------------------ epilogue
+    // 8 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 of tile (w - 2) / 4
     const int quad = warp & 3;
+    const int tile = (warp - 2) >> 2;
     const int row = quad * 32 + lane;
+    const int prow = tile * kTileM + row;                 // point within the pair
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
     // l_ij scratch of this CTA: [pair parity][component][256 points of the pair]
-    float *scr = lsc + (size_t)blockIdx.x * 2 * K * (2 * kTileM);
+    float *scr = lsc + (size_t)blockIdx.x * 2 * K * (2 * kTileM) + prow;
     double lsum = 0.0;
     bool ok = true;
     bool have_prev = false;
     int prev_par = 0;
-    int64_t prev_i[2] = {-1, -1};
-    float prev_lse[2] = {0.f, 0.f};
+    int64_t prev_i = -1;
+    float prev_lse = 0.f;
     uint32_t ai = 0;
     int pc = 0;
     for (int64_t pr = blockIdx.x; pr < npairs && ok; pr += gridDim.x, pc++) {
       const int par = pc & 1;
-      const int nt = (2 * pr + 1 < ntiles) ? 2 : 1;
-      int64_t pi[2];
-      float mx[2] = {-INFINITY, -INFINITY}, se[2] = {0.f, 0.f}, smax[2] = {0.f, 0.f};
-      int jmax[2] = {0, 0};
-      for (int t = 0; t < 2; t++) pi[t] = (t < nt && (2 * pr + t) * kTileM + row < n) ? (2 * pr + t) * kTileM + row : -1;
+      const bool live = tile < ((2 * pr + 1 < ntiles) ? 2 : 1);   // warp-uniform
+      const int64_t pi = (live && (2 * pr + tile) * kTileM + row < n) ? (2 * pr + tile) * kTileM + row : -1;
+      float mx = -INFINITY, se = 0.f, smax = 0.f;
+      int jmax = 0;
       for (int g = 0; g < G; g++) {
         // posteriors of components 2g, 2g+1 of the previous pair: load early
-        float lp[2][2];
-        if (have_prev) {
+        float lp[2] = {0.f, 0.f};
+        if (have_prev && prev_i >= 0) {
 #pragma unroll
-          for (int t = 0; t < 2; t++)
-#pragma unroll
-            for (int q = 0; q < 2; q++)
-              lp[t][q] = scr[((size_t)(prev_par * K + 2 * g + q)) * (2 * kTileM) + t * kTileM + row];
+          for (int q = 0; q < 2; q++) lp[q] = scr[(size_t)(prev_par * K + 2 * g + q) * (2 * kTileM)];
         }
         const int ab = ai & 1;
-        // warp-uniform outcome: the TMEM loads below are .sync.aligned
-        if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (ai >> 1) & 1, err)))) break;
+        if (!(ok = mbar_wait_warp(&S.acc_full[ab], (ai >> 1) & 1, err))) break;
         tc_fence_after();
-        float s[2][kCompPerGroup] = {{0.f, 0.f}, {0.f, 0.f}};
-        const float *bg = S.bias + g * kGroupN;
-        // 32-column block bp holds k-block (3 - bp) of both components:
-        // column 32 bp + 16 q + t belongs to component q
+        float s[kCompPerGroup] = {0.f, 0.f};
+        if (live) {
+          const float *bg = S.bias + g * kGroupN;
+          // 32-column block bp holds k-block (3 - bp) of both components:
+          // column 32 bp + 16 q + t belongs to component q
 #pragma unroll 1
-        for (int bp = 0; bp < kGroupN / 32; bp++) {
-          uint32_t v[2][32];
-          tmem_ld32(tbase + lane_addr + (2 * ab) * kGroupN + bp * 32, v[0]);
-          if (nt > 1) tmem_ld32(tbase + lane_addr + (2 * ab + 1) * kGroupN + bp * 32, v[1]);
-          float4 b[8];
-          const float4 *b4 = reinterpret_cast<const float4 *>(bg + bp * 32);
+          for (int bp = 0; bp < kGroupN / 32; bp++) {
+            uint32_t v[32];
+            tmem_ld32(tbase + lane_addr + (2 * ab + tile) * kGroupN + bp * 32, v);
+            float4 b[8];
+            const float4 *b4 = reinterpret_cast<const float4 *>(bg + bp * 32);
 #pragma unroll
-          for (int u = 0; u < 8; u++) b[u] = b4[u];
-          tmem_wait_ld();
+            for (int u = 0; u < 8; u++) b[u] = b4[u];
+            tmem_wait_ld();
 #pragma unroll
-          for (int t = 0; t < 32; t++) {
-            const float bb = (t & 3) == 0 ? b[t >> 2].x : (t & 3) == 1 ? b[t >> 2].y
-                           : (t & 3) == 2 ? b[t >> 2].z : b[t >> 2].w;
-            const float y0 = __uint_as_float(v[0][t]) - bb;
-            s[0][t >> 4] = fmaf(y0, y0, s[0][t >> 4]);
-            if (nt > 1) {
-              const float y1 = __uint_as_float(v[1][t]) - bb;
-              s[1][t >> 4] = fmaf(y1, y1, s[1][t >> 4]);
+            for (int t = 0; t < 32; t++) {
+              const float bb = (t & 3) == 0 ? b[t >> 2].x : (t & 3) == 1 ? b[t >> 2].y
+                             : (t & 3) == 2 ? b[t >> 2].z : b[t >> 2].w;
+              const float y = __uint_as_float(v[t]) - bb;
+              s[t >> 4] = fmaf(y, y, s[t >> 4]);
             }
           }
         }
@@ -318,66 +313,58 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         __syncwarp();
         if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
         ai++;
-        if (have_prev) {
+        if (have_prev && prev_i >= 0) {
 #pragma unroll
-          for (int t = 0; t < 2; t++)
-            if (prev_i[t] >= 0)
-#pragma unroll
-              for (int q = 0; q < 2; q++)
-                store_post(Rh, Rl, (size_t)(2 * g + q) * np + prev_i[t], expf(lp[t][q] - prev_lse[t]));
+          for (int q = 0; q < 2; q++) store_post(Rh, Rl, (size_t)(2 * g + q) * np + prev_i, expf(lp[q] - prev_lse));
         }
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
+        if (live) {
 #pragma unroll
           for (int q = 0; q < kCompPerGroup; q++) {
             const int j = g * kCompPerGroup + q;
             // c_j carried as float hi + lo: its rounding would shift every
             // posterior of component j by the same factor
-            const float l = (S.chi[j] - 0.5f * s[t][q]) + S.clo[j];
-            scr[((size_t)(par * K + j)) * (2 * kTileM) + t * kTileM + row] = l;
-            if (l > mx[t]) {
-              se[t] = se[t] * __expf(mx[t] - l) + 1.f;
-              mx[t] = l;
-              jmax[t] = j;
-              smax[t] = s[t][q];
+            const float l = (S.chi[j] - 0.5f * s[q]) + S.clo[j];
+            scr[(size_t)(par * K + j) * (2 * kTileM)] = l;
+            if (l > mx) {
+              se = se * __expf(mx - l) + 1.f;
+              mx = l;
+              jmax = j;
+              smax = s[q];
             } else if (l > -INFINITY) {
-              se[t] += __expf(l - mx[t]);
+              se += __expf(l - mx);
             }
           }
         }
       }
       if (!ok) break;
-#pragma unroll
-      for (int t = 0; t < 2; t++) {
-        prev_i[t] = pi[t];
-        prev_lse[t] = mx[t] + __logf(se[t]);
-        if (pi[t] >= 0) lsum += c64[jmax[t]] - 0.5 * (double)smax[t] + (double)__logf(se[t]);
-      }
+      prev_i = pi;
+      prev_lse = mx + __logf(se);
+      if (pi >= 0) lsum += c64[jmax] - 0.5 * (double)smax + (double)__logf(se);
       prev_par = par;
       have_prev = true;
     }
     // posteriors of the last pair
-    if (ok && have_prev) {
+    if (ok && have_prev && prev_i >= 0) {
+      for (int j0 = 0; j0 < K; j0 += 8) {
+        float l8[8];
 #pragma unroll
-      for (int t = 0; t < 2; t++) {
-        if (prev_i[t] < 0) continue;
-        for (int j0 = 0; j0 < K; j0 += 8) {
-          float l8[8];
+        for (int u = 0; u < 8; u++)
+          l8[u] = (j0 + u < K) ? scr[(size_t)(prev_par * K + j0 + u) * (2 * kTileM)] : 0.f;
 #pragma unroll
-          for (int u = 0; u < 8; u++)
-            l8[u] = (j0 + u < K) ? scr[((size_t)(prev_par * K + j0 + u)) * (2 * kTileM) + t * kTileM + row] : 0.f;
-#pragma unroll
-          for (int u = 0; u < 8; u++)
-            if (j0 + u < K) store_post(Rh, Rl, (size_t)(j0 + u) * np + prev_i[t], expf(l8[u] - prev_lse[t]));
-        }
+        for (int u = 0; u < 8; u++)
+          if (j0 + u < K) store_post(Rh, Rl, (size_t)(j0 + u) * np + prev_i, expf(l8[u] - prev_lse));
       }
     }
-    // deterministic reduction over the 128 epilogue threads
+    // deterministic reduction over the 256 epilogue threads
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-    if (lane == 0) S.red[quad] = lsum;
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    if (threadIdx.x == 64) part[blockIdx.x] = S.red[0] + S.red[1] + S.red[2] + S.red[3];
+    if (lane == 0) S.red[warp - 2] = lsum;
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+    if (threadIdx.x == 64) {
+      double t = 0.0;
+      for (int w = 0; w < 8; w++) t += S.red[w];
+      part[blockIdx.x] = t;
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -480,7 +467,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
       const int ab = w & 1;
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (w >> 1) & 1, err)))) break;
+      if (!(ok = mbar_wait_warp(&S.acc_full[ab], (w >> 1) & 1, err))) break;
       tc_fence_after();
       const uint32_t ta = tbase + ((uint32_t)(quad * 32) << 16) + ab * 128;
 #pragma unroll 1
@@ -618,8 +605,8 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
       const int si = (int)(tb % kCIn), sz = tb & 1;
-      bool got = mbar_wait(&S.in_full[si], (tb / kCIn) & 1, err);
-      got = got && mbar_wait(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err);
+      bool got = mbar_wait_warp(&S.in_full[si], (tb / kCIn) & 1, err);
+      got = got && mbar_wait_warp(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err);
       // sqrt(r) of (component t / 64, point t % 64), r = rh + rl
       if (got) S.sr[sz][t] = sqrtf(__half2float(S.rh[si][t]) + __half2float(S.rl[si][t]));
       // one decision for all 256 producers (they meet at this barrier every block)
@@ -690,7 +677,7 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
       const int ab = w & 1;
-      if (!(ok = __all_sync(0xffffffffu, mbar_wait(&S.acc_full[ab], (w >> 1) & 1, err)))) break;
+      if (!(ok = mbar_wait_warp(&S.acc_full[ab], (w >> 1) & 1, err))) break;
       tc_fence_after();
 #pragma unroll 1
       for (int pc = 0; pc < 4; pc++) {          // (pair, 32-column chunk)

@@ -48,19 +48,45 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait for the phase with the given parity to complete
+// try_wait that lets the hardware suspend the thread for up to `ns`
+// nanoseconds while the phase is incomplete (no busy spinning)
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait for the phase with the given parity to complete; the error
+// flag and the clock budget are checked every 16 suspended tries
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
   while (true) {
+#pragma unroll 1
+    for (int i = 0; i < 16; i++)
+      if (mbar_try_wait_sleep(a, parity, 2000)) return true;
     if (*(volatile int *)err) return false;
-    if (mbar_try_wait(a, parity)) return true;
     if (clock64() - t0 > kWaitBudgetCycles) {
       atomicExch(err, 1);
       return false;
     }
   }
+}
+
+// warp-wide bounded wait: lane 0 waits, the outcome is broadcast (use
+// before .sync.aligned tcgen05 instructions)
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, int *err) {
+  uint32_t ok = 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err);
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
 }
 
 // bounded wait that ignores the error flag: used to drain copies / MMAs
