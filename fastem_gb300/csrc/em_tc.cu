@@ -100,7 +100,7 @@ struct __align__(1024) CSmem {
   float xs[kCIn][kBlk * kD];     // X tile (points x dims)
   __half rh[kCIn][4 * kBlk];
   __half rl[kCIn][4 * kBlk];
-  float sr[2][4 * kBlk];         // sqrt(r)
+  float sr[8][4 * 16];           // per producer warp: sqrt(r) of its 16 points x 4 components
   double dred[4][4][kD];         // exact-diagonal partials of the 4 point slices
   uint64_t in_full[kCIn], in_empty[kCIn], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
   uint32_t tmem_base;
@@ -145,7 +145,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
            const double *__restrict__ c64, float *__restrict__ lsc, __half *__restrict__ Rh,
            __half *__restrict__ Rl, int64_t np, double *__restrict__ part, int64_t n, int K, int *err) {
   extern __shared__ uint8_t smem_raw[];
-  ESmem &S = *reinterpret_cast<ESmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  ESmem &S = smem_aligned<ESmem>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = K / kCompPerGroup;
   const int64_t ntiles = (n + kTileM - 1) / kTileM;
@@ -382,7 +382,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
            const __grid_constant__ CUtensorMap tm_xht, const __grid_constant__ CUtensorMap tm_xlt,
            int64_t n, double *__restrict__ part, int *err) {
   extern __shared__ uint8_t smem_raw[];
-  MSmem &S = *reinterpret_cast<MSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  MSmem &S = smem_aligned<MSmem>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t nblocks = (n + kBlk - 1) / kBlk;
   // blocks of this CTA: b = blockIdx.x + t * gridDim.x, t < mine
@@ -523,7 +523,7 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
          const __grid_constant__ CUtensorMap tm_rl4, const float *__restrict__ muf, int64_t n,
          int64_t blocks_per_chunk, double *__restrict__ cpart, double *__restrict__ dpart, int *err) {
   extern __shared__ uint8_t smem_raw[];
-  CSmem &S = *reinterpret_cast<CSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  CSmem &S = smem_aligned<CSmem>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int grp = blockIdx.x;
   const int64_t nblocks = (n + kBlk - 1) / kBlk;
@@ -594,55 +594,65 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
   } else if (warp < 10) {
     // ------------------------------------------------ producers
     // thread t: dimension a = t % 64 and the 16-point slice pc = t / 64 of
-    // the block, for all 4 components (x is read once per point)
+    // the block, for all 4 components (x is read once per point). Each warp
+    // computes sqrt(r) of its own 16 points x 4 components (two per lane)
+    // into its own slot, so producers synchronise only through mbarriers.
     const int t = threadIdx.x - 64;             // 0..255
     const int a = t & 63, pc = t >> 6;
-    float mu_a[4];
+    float *srw = S.sr[warp - 2];
+    float2 nmu[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) mu_a[q] = muf[(size_t)(grp * 4 + q) * kD + a];
+    for (int q = 0; q < 4; q++) {
+      const float m = muf[(size_t)(grp * 4 + q) * kD + a];
+      nmu[q] = make_float2(-m, -m);
+    }
     double diag[4] = {0.0, 0.0, 0.0, 0.0};
-    float dwin[4] = {0.f, 0.f, 0.f, 0.f};
+    float2 dwin[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) dwin[q] = make_float2(0.f, 0.f);
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
       const int si = (int)(tb % kCIn), sz = tb & 1;
-      bool got = mbar_wait_warp(&S.in_full[si], (tb / kCIn) & 1, err);
-      got = got && mbar_wait_warp(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err);
-      // sqrt(r) of (component t / 64, point t % 64), r = rh + rl
-      if (got) S.sr[sz][t] = sqrtf(__half2float(S.rh[si][t]) + __half2float(S.rl[si][t]));
-      // one decision for all 256 producers (they meet at this barrier every block)
-      if (!(ok = bar_and(2, 256, got))) break;
-      const float *xr = S.xs[si];
+      if (!(ok = mbar_wait_warp(&S.in_full[si], (tb / kCIn) & 1, err))) break;
       const int64_t pbase = (b0 + tb) * kBlk;
+      {
+        // lane -> component lane / 8, points 2 (lane % 8) + {0, 1} of the slice;
+        // rows past N read zero-filled r and x, and get s = 0 besides
+        const int q = lane >> 3, p = pc * 16 + 2 * (lane & 7);
+        const float2 rh = __half22float2(*reinterpret_cast<const __half2 *>(&S.rh[si][q * kBlk + p]));
+        const float2 rl = __half22float2(*reinterpret_cast<const __half2 *>(&S.rl[si][q * kBlk + p]));
+        const float s0 = (pbase + p < n) ? sqrtf(rh.x + rl.x) : 0.f;
+        const float s1 = (pbase + p + 1 < n) ? sqrtf(rh.y + rl.y) : 0.f;
+        __syncwarp();                           // the previous block's reads of the slot are done
+        *reinterpret_cast<float2 *>(srw + q * 16 + 2 * (lane & 7)) = make_float2(s0, s1);
+        __syncwarp();
+      }
+      if (!(ok = mbar_wait_warp(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err))) break;
+      const float *xr = S.xs[si] + (pc * 16) * kD + a;
+      float2 xv[8];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {             // two 8-point chunks of the slice
-        const int c8 = pc * 2 + h;
-        float xv[8];
+      for (int u = 0; u < 8; u++) xv[u] = make_float2(xr[(2 * u) * kD], xr[(2 * u + 1) * kD]);
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-          const int p = c8 * 8 + u;
-          // rows past N are zero-filled in xs and r; keep them exactly zero
-          xv[u] = (pbase + p < n) ? xr[p * kD + a] : 0.f;
-        }
+      for (int q = 0; q < 4; q++) {
+        const float4 *s4 = reinterpret_cast<const float4 *>(srw + q * 16);
+        uint32_t w8[8];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          const float *sq = S.sr[sz] + q * kBlk + c8 * 8;
-          const float4 sa = *reinterpret_cast<const float4 *>(sq);
-          const float4 sb = *reinterpret_cast<const float4 *>(sq + 4);
-          const float sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
-          uint32_t w4[4];
+        for (int v = 0; v < 4; v++) {
+          const float4 sv = s4[v];
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const float z0 = (xv[2 * u] - mu_a[q]) * sv[2 * u];
-            const float z1 = (xv[2 * u + 1] - mu_a[q]) * sv[2 * u + 1];
-            dwin[q] = fmaf(z0, z0, dwin[q]);
-            dwin[q] = fmaf(z1, z1, dwin[q]);
-            const __half2 hz = __floats2half2_rn(z0, z1);
-            w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+          for (int e = 0; e < 2; e++) {
+            const int u = 2 * v + e;
+            const float2 s2 = e ? make_float2(sv.z, sv.w) : make_float2(sv.x, sv.y);
+            const float2 z = __fmul2_rn(__fadd2_rn(xv[u], nmu[q]), s2);
+            dwin[q] = __ffma2_rn(z, z, dwin[q]);
+            const __half2 hz = __floats2half2_rn(z.x, z.y);
+            w8[u] = *reinterpret_cast<const uint32_t *>(&hz);
           }
-          const int row = ((q & 1) << 6) + a;
-          uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
-          *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
         }
+        const int row = ((q & 1) << 6) + a;
+        uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
+        *reinterpret_cast<uint4 *>(zrow + (((2 * pc) ^ (row & 7)) << 4)) = make_uint4(w8[0], w8[1], w8[2], w8[3]);
+        *reinterpret_cast<uint4 *>(zrow + (((2 * pc + 1) ^ (row & 7)) << 4)) = make_uint4(w8[4], w8[5], w8[6], w8[7]);
       }
       fence_proxy_async_smem();
       __syncwarp();
@@ -652,12 +662,14 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
       }
       if ((tb + 1) % kFlushBlocks == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q], dwin[q] = 0.f;
+        for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q].x + (double)dwin[q].y, dwin[q] = make_float2(0.f, 0.f);
       }
     }
+#pragma unroll
+    for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q].x + (double)dwin[q].y;
     // exact diagonal: combine the 4 point slices in a fixed order
 #pragma unroll
-    for (int q = 0; q < 4; q++) S.dred[pc][q][a] = diag[q] + (double)dwin[q];
+    for (int q = 0; q < 4; q++) S.dred[pc][q][a] = diag[q];
     asm volatile("bar.sync 2, 256;" ::: "memory");
     if (pc == 0)
 #pragma unroll

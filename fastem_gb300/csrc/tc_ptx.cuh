@@ -19,6 +19,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// the dynamic shared-memory window rounded up to a 1024-byte boundary (the
+// 128-byte swizzle atoms need it). The pointer stays derived from the
+// __shared__ array by plain offsets, so accesses through it compile to
+// shared-memory loads and stores rather than generic ones.
+template <class T>
+__device__ __forceinline__ T &smem_aligned(uint8_t *raw) {
+  return *reinterpret_cast<T *>(raw + ((1024u - (smem_u32(raw) & 1023u)) & 1023u));
+}
+
 // ------------------------------------------------------------- mbarrier
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -62,15 +71,15 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parit
 }
 
 // bounded wait for the phase with the given parity to complete; the error
-// flag and the clock budget are checked every 16 suspended tries
+// flag and the clock budget are checked every 64 tries
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
   while (true) {
 #pragma unroll 1
-    for (int i = 0; i < 16; i++)
-      if (mbar_try_wait_sleep(a, parity, 2000)) return true;
+    for (int i = 0; i < 64; i++)
+      if (mbar_try_wait(a, parity)) return true;
     if (*(volatile int *)err) return false;
     if (clock64() - t0 > kWaitBudgetCycles) {
       atomicExch(err, 1);
