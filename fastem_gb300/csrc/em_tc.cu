@@ -95,17 +95,21 @@ struct __align__(1024) MSmem {
 };
 
 // covariance kernel: 4 components per CTA (2 pairs), 64-point blocks
+constexpr int kZStages = 3;              // operand (z) ring
+constexpr int kCProd = 16;               // producer warps: 2 dimension halves x 8 point chunks
 struct __align__(1024) CSmem {
-  __half z[2][2][128 * kBlk];    // [stage][pair] 128 rows (comp q dims) x 64 points, SW128
+  __half z[kZStages][2][128 * kBlk];  // [stage][pair] 128 rows (comp q dims) x 64 points, SW128
   float xs[kCIn][kBlk * kD];     // X tile (points x dims)
   __half rh[kCIn][4 * kBlk];
   __half rl[kCIn][4 * kBlk];
-  float sr[8][4 * 16];           // per producer warp: sqrt(r) of its 16 points x 4 components
-  double dred[4][4][kD];         // exact-diagonal partials of the 4 point slices
-  uint64_t in_full[kCIn], in_empty[kCIn], z_full[2], z_empty[2], acc_full[2], acc_empty[2], mma_done;
+  float sr[kCProd][4 * 8];       // per producer warp: sqrt(r) of its 8 points x 4 components
+  double dred[8][4][kD];         // exact-diagonal partials of the 8 point chunks
+  uint64_t in_full[kCIn], in_empty[kCIn], z_full[kZStages], z_empty[kZStages], acc_full[2], acc_empty[2],
+      mma_done;
   uint32_t tmem_base;
 };
-constexpr int kCThreads = 448;   // warp 0 TMA, 1 MMA, 2..9 producers, 10..13 flush
+constexpr int kCThreads = (2 + kCProd + 4) * 32;   // warp 0 TMA, 1 MMA, 2..17 producers, 18..21 flush
+static_assert(sizeof(CSmem) + 1024 <= 232448, "covariance kernel shared memory");
 
 struct TcEmPlan {
   CUtensorMap tm_xh, tm_xl, tm_wh, tm_wl;      // E-step
@@ -176,7 +180,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
       uint32_t xi = 0, wi = 0;
       bool ok = true;
       for (int64_t pr = blockIdx.x; pr < npairs && ok; pr += gridDim.x) {
-        if (!(ok = mbar_wait(&S.x_empty, (xi & 1) ^ 1, err))) break;
+        if (!(ok = mbar_wait_lazy(&S.x_empty, (xi & 1) ^ 1, err, 128))) break;
         const bool has1 = 2 * pr + 1 < ntiles;
         mbar_expect_tx(&S.x_full, (has1 ? 4 : 2) * kXBytes);
         tma_load_2d(S.xh[0], &tm_xh, &S.x_full, 0, (int)(2 * pr * kTileM));
@@ -188,7 +192,7 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         xi++;
         for (int g = 0; g < G; g++) {
           const int ws = wi % kWStages;
-          if (!(ok = mbar_wait(&S.w_empty[ws], ((wi / kWStages) & 1) ^ 1, err))) break;
+          if (!(ok = mbar_wait_lazy(&S.w_empty[ws], ((wi / kWStages) & 1) ^ 1, err, 128))) break;
           mbar_expect_tx(&S.w_full[ws], 2 * kWBytes);
           tma_load_2d(S.wh[ws], &tm_wh, &S.w_full[ws], 0, g * kGroupN);
           tma_load_2d(S.wl[ws], &tm_wl, &S.w_full[ws], 0, g * kGroupN);
@@ -417,7 +421,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
       bool ok = true;
       for (int64_t t = 0; t < mine && ok; t++) {
         const int s = (int)(t % kMStages);
-        if (!(ok = mbar_wait(&S.in_empty[s], ((t / kMStages) & 1) ^ 1, err))) break;
+        if (!(ok = mbar_wait_lazy(&S.in_empty[s], ((t / kMStages) & 1) ^ 1, err, 128))) break;
         const int p0 = (int)((blockIdx.x + t * gridDim.x) * kBlk);
         mbar_expect_tx(&S.in_full[s], kInBytes);
         tma_load_2d(S.rh[s], &tm_rh, &S.in_full[s], p0, 0);
@@ -467,7 +471,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
       const int ab = w & 1;
-      if (!(ok = mbar_wait_warp(&S.acc_full[ab], (w >> 1) & 1, err))) break;
+      if (!(ok = mbar_wait_lazy_warp(&S.acc_full[ab], (w >> 1) & 1, err, 1000))) break;
       tc_fence_after();
       const uint32_t ta = tbase + ((uint32_t)(quad * 32) << 16) + ab * 128;
 #pragma unroll 1
@@ -515,9 +519,10 @@ __global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, 
 
 // ========================================================= covariances
 // CTA (blockIdx.x = group of 4 components, blockIdx.y = chunk of points).
-// Producer thread t (warps 2..9): component q = t / 64 of the group, dim
-// a = t % 64; it writes row (q % 2) * 64 + a of pair q / 2's operand tile
-// (8 points per 16-byte store, 128-byte swizzle) and sums z^2 exactly.
+// Producer thread (warps 2..17): dimension a, 8-point chunk c8; for each of
+// the 4 components q it writes z = sqrt(r) (x - mu) of its 8 points as one
+// 16-byte store into row (q % 2) * 64 + a of pair q / 2's operand tile
+// (128-byte swizzle) and sums z^2 in FP32 / FP64 for the exact diagonal.
 __global__ void __launch_bounds__(kCThreads, 1)
 k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUtensorMap tm_rh4,
          const __grid_constant__ CUtensorMap tm_rl4, const float *__restrict__ muf, int64_t n,
@@ -533,11 +538,9 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
   const size_t cta = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kCIn; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], 8);
-    for (int s = 0; s < 2; s++) {
-      mbar_init(&S.z_full[s], 8), mbar_init(&S.z_empty[s], 1);
-      mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
-    }
+    for (int s = 0; s < kCIn; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], kCProd);
+    for (int s = 0; s < kZStages; s++) mbar_init(&S.z_full[s], kCProd), mbar_init(&S.z_empty[s], 1);
+    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
   }
@@ -553,7 +556,7 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
       bool ok = true;
       for (int64_t t = 0; t < mine && ok; t++) {
         const int s = (int)(t % kCIn);
-        if (!(ok = mbar_wait(&S.in_empty[s], ((t / kCIn) & 1) ^ 1, err))) break;
+        if (!(ok = mbar_wait_lazy(&S.in_empty[s], ((t / kCIn) & 1) ^ 1, err, 128))) break;
         const int p0 = (int)((b0 + t) * kBlk);
         mbar_expect_tx(&S.in_full[s], kInBytes);
         tma_load_2d(S.xs[s], &tm_x32, &S.in_full[s], 0, p0);
@@ -572,8 +575,8 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         if (!(ok = mbar_wait(&S.acc_empty[ab], ((w >> 1) & 1) ^ 1, err))) break;
         const int64_t t1 = std::min<int64_t>(mine, (w + 1) * kFlushBlocks);
         for (int64_t t = w * kFlushBlocks; t < t1; t++) {
-          const int s = t & 1;
-          if (!(ok = mbar_wait(&S.z_full[s], (t >> 1) & 1, err))) break;
+          const int s = (int)(t % kZStages);
+          if (!(ok = mbar_wait(&S.z_full[s], (t / kZStages) & 1, err))) break;
           tc_fence_after();
 #pragma unroll
           for (int pr = 0; pr < 2; pr++) {
@@ -591,14 +594,14 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
       mma_commit(&S.mma_done);
       mbar_wait_drain(&S.mma_done, 0);
     }
-  } else if (warp < 10) {
+  } else if (warp < 2 + kCProd) {
     // ------------------------------------------------ producers
-    // thread t: dimension a = t % 64 and the 16-point slice pc = t / 64 of
+    // thread t: dimension a = t % 64 and the 8-point chunk c8 = t / 64 of
     // the block, for all 4 components (x is read once per point). Each warp
-    // computes sqrt(r) of its own 16 points x 4 components (two per lane)
+    // computes sqrt(r) of its own 8 points x 4 components (one per lane)
     // into its own slot, so producers synchronise only through mbarriers.
-    const int t = threadIdx.x - 64;             // 0..255
-    const int a = t & 63, pc = t >> 6;
+    const int t = threadIdx.x - 64;             // 0..511
+    const int a = t & 63, c8 = t >> 6;
     float *srw = S.sr[warp - 2];
     float2 nmu[4];
 #pragma unroll
@@ -612,47 +615,40 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     for (int q = 0; q < 4; q++) dwin[q] = make_float2(0.f, 0.f);
     bool ok = true;
     for (int64_t tb = 0; tb < mine && ok; tb++) {
-      const int si = (int)(tb % kCIn), sz = tb & 1;
+      const int si = (int)(tb % kCIn), sz = (int)(tb % kZStages);
       if (!(ok = mbar_wait_warp(&S.in_full[si], (tb / kCIn) & 1, err))) break;
-      const int64_t pbase = (b0 + tb) * kBlk;
       {
-        // lane -> component lane / 8, points 2 (lane % 8) + {0, 1} of the slice;
-        // rows past N read zero-filled r and x, and get s = 0 besides
-        const int q = lane >> 3, p = pc * 16 + 2 * (lane & 7);
-        const float2 rh = __half22float2(*reinterpret_cast<const __half2 *>(&S.rh[si][q * kBlk + p]));
-        const float2 rl = __half22float2(*reinterpret_cast<const __half2 *>(&S.rl[si][q * kBlk + p]));
-        const float s0 = (pbase + p < n) ? sqrtf(rh.x + rl.x) : 0.f;
-        const float s1 = (pbase + p + 1 < n) ? sqrtf(rh.y + rl.y) : 0.f;
+        // lane -> component lane / 8, point c8 * 8 + lane % 8; rows past N
+        // read zero-filled r and x, and get s = 0 besides
+        const int q = lane >> 3, p = c8 * 8 + (lane & 7);
+        const float r = __half2float(S.rh[si][q * kBlk + p]) + __half2float(S.rl[si][q * kBlk + p]);
+        const float sv = ((b0 + tb) * kBlk + p < n) ? sqrtf(r) : 0.f;
         __syncwarp();                           // the previous block's reads of the slot are done
-        *reinterpret_cast<float2 *>(srw + q * 16 + 2 * (lane & 7)) = make_float2(s0, s1);
+        srw[lane] = sv;
         __syncwarp();
       }
-      if (!(ok = mbar_wait_warp(&S.z_empty[sz], ((tb >> 1) & 1) ^ 1, err))) break;
-      const float *xr = S.xs[si] + (pc * 16) * kD + a;
-      float2 xv[8];
+      const float *xr = S.xs[si] + (c8 * 8) * kD + a;
+      float2 xv[4];
 #pragma unroll
-      for (int u = 0; u < 8; u++) xv[u] = make_float2(xr[(2 * u) * kD], xr[(2 * u + 1) * kD]);
+      for (int u = 0; u < 4; u++) xv[u] = make_float2(xr[(2 * u) * kD], xr[(2 * u + 1) * kD]);
+      if (!(ok = mbar_wait_warp(&S.z_empty[sz], ((tb / kZStages) & 1) ^ 1, err))) break;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
-        const float4 *s4 = reinterpret_cast<const float4 *>(srw + q * 16);
-        uint32_t w8[8];
+        const float4 s0 = *reinterpret_cast<const float4 *>(srw + q * 8);
+        const float4 s1 = *reinterpret_cast<const float4 *>(srw + q * 8 + 4);
+        const float2 s2[4] = {make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y),
+                              make_float2(s1.z, s1.w)};
+        uint32_t w4[4];
 #pragma unroll
-        for (int v = 0; v < 4; v++) {
-          const float4 sv = s4[v];
-#pragma unroll
-          for (int e = 0; e < 2; e++) {
-            const int u = 2 * v + e;
-            const float2 s2 = e ? make_float2(sv.z, sv.w) : make_float2(sv.x, sv.y);
-            const float2 z = __fmul2_rn(__fadd2_rn(xv[u], nmu[q]), s2);
-            dwin[q] = __ffma2_rn(z, z, dwin[q]);
-            const __half2 hz = __floats2half2_rn(z.x, z.y);
-            w8[u] = *reinterpret_cast<const uint32_t *>(&hz);
-          }
+        for (int u = 0; u < 4; u++) {
+          const float2 z = __fmul2_rn(__fadd2_rn(xv[u], nmu[q]), s2[u]);
+          dwin[q] = __ffma2_rn(z, z, dwin[q]);
+          const __half2 hz = __floats2half2_rn(z.x, z.y);
+          w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
         }
         const int row = ((q & 1) << 6) + a;
         uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
-        *reinterpret_cast<uint4 *>(zrow + (((2 * pc) ^ (row & 7)) << 4)) = make_uint4(w8[0], w8[1], w8[2], w8[3]);
-        *reinterpret_cast<uint4 *>(zrow + (((2 * pc + 1) ^ (row & 7)) << 4)) = make_uint4(w8[4], w8[5], w8[6], w8[7]);
+        *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
       }
       fence_proxy_async_smem();
       __syncwarp();
@@ -667,16 +663,19 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q].x + (double)dwin[q].y;
-    // exact diagonal: combine the 4 point slices in a fixed order
+    // exact diagonal: combine the 8 point chunks in a fixed order
 #pragma unroll
-    for (int q = 0; q < 4; q++) S.dred[pc][q][a] = diag[q];
-    asm volatile("bar.sync 2, 256;" ::: "memory");
-    if (pc == 0)
+    for (int q = 0; q < 4; q++) S.dred[c8][q][a] = diag[q];
+    asm volatile("bar.sync 2, %0;" ::"n"(kCProd * 32) : "memory");
+    if (c8 == 0)
 #pragma unroll
-      for (int q = 0; q < 4; q++)
-        dpart[(cta * 4 + q) * kD + a] = ((S.dred[0][q][a] + S.dred[1][q][a]) + S.dred[2][q][a]) + S.dred[3][q][a];
+      for (int q = 0; q < 4; q++) {
+        double v = S.dred[0][q][a];
+        for (int c = 1; c < 8; c++) v += S.dred[c][q][a];
+        dpart[(cta * 4 + q) * kD + a] = v;
+      }
   } else {
-    // ------------------------------------------------ flush warps 10..13
+    // ------------------------------------------------ flush warps 18..21
     const int quad = warp & 3;
     const int lrow = quad * 32 + lane;          // TMEM lane = row of the pair tile
     const int half = lrow >> 6;                 // 0: first component of the pair, 1: second
@@ -689,16 +688,18 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
       const int ab = w & 1;
-      if (!(ok = mbar_wait_warp(&S.acc_full[ab], (w >> 1) & 1, err))) break;
+      if (!(ok = mbar_wait_lazy_warp(&S.acc_full[ab], (w >> 1) & 1, err, 1000))) break;
       tc_fence_after();
-#pragma unroll 1
-      for (int pc = 0; pc < 4; pc++) {          // (pair, 32-column chunk)
-        const int pr = pc >> 1, c0 = (pc & 1) * 32;
-        uint32_t v[32];
-        tmem_ld32(tbase + ((uint32_t)(quad * 32) << 16) + ab * 256 + pr * 128 + half * 64 + c0, v);
-        tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < 32; c++) o[pr][c0 + c] += (double)__uint_as_float(v[c]);
+      for (int pr = 0; pr < 2; pr++) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < kD; c0 += 32) {   // 32-column chunks
+          uint32_t v[32];
+          tmem_ld32(tbase + ((uint32_t)(quad * 32) << 16) + ab * 256 + pr * 128 + half * 64 + c0, v);
+          tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 32; c++) o[pr][c0 + c] += (double)__uint_as_float(v[c]);
+        }
       }
       tc_fence_before();
       __syncwarp();

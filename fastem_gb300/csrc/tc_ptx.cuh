@@ -98,6 +98,33 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, i
   return ok != 0;
 }
 
+// bounded wait for waiters off the critical path (flush warps that act once
+// per window, TMA threads with several stages of slack): between tries the
+// thread sleeps `ns` nanoseconds, so its polling does not take shared-memory
+// pipe slots from the warps that are doing the work
+__device__ __forceinline__ bool mbar_wait_lazy(uint64_t *bar, uint32_t parity, int *err, unsigned ns) {
+  const uint32_t a = smem_u32(bar);
+  if (mbar_try_wait(a, parity)) return true;
+  const long long t0 = clock64();
+  while (true) {
+    __nanosleep(ns);
+    if (mbar_try_wait(a, parity)) return true;
+    if (*(volatile int *)err) return false;
+    if (clock64() - t0 > kWaitBudgetCycles) {
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ bool mbar_wait_lazy_warp(uint64_t *bar, uint32_t parity, int *err, unsigned ns) {
+  uint32_t ok = 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_lazy(bar, parity, err, ns);
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+
 // bounded wait that ignores the error flag: used to drain copies / MMAs
 // still in flight before shared memory and TMEM are released
 __device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity) {
