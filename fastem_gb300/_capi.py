@@ -31,6 +31,7 @@ EXPORTS = [
     "fem_em_train", "fem_em_init_densities", "fem_em_precompute", "fem_em_mstep",
     "fem_em_max_condition", "fem_em_get_posteriors", "fem_em_retrieve_classes",
     "fem_em_get_factors", "fem_em_timing_reset", "fem_em_timing_get", "fem_em_timing_total",
+    "fem_em_timing_covariance",
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
@@ -98,6 +99,7 @@ def lib():
         "fem_em_timing_reset": ([P, i32], i32),
         "fem_em_timing_get": ([P, P, P, P, P], i32),
         "fem_em_timing_total": ([P, P, P], i32),
+        "fem_em_timing_covariance": ([P, P], i32),
         "fem_km_config_default": ([ctypes.POINTER(KmConfig)], None),
         "fem_km_create": ([i32, i64, i32, ctypes.POINTER(KmConfig), pP], i32),
         "fem_km_destroy": ([P], None),

@@ -17,6 +17,13 @@
 
 using namespace fem;
 
+void fem::timing_begin(fem_em *h, int slot) {
+  if (h->timing) {
+    cudaEventRecord(h->ev[slot], h->stream);
+    h->tmask |= 1u << slot;
+  }
+}
+
 namespace {
 
 int check_handle(fem_em *h) {
@@ -29,23 +36,16 @@ int check_handle(fem_em *h) {
 
 bool mixed(const fem_em *h) { return h->cfg.precision == FEM_PREC_MIXED; }
 
-void timing_begin(fem_em *h, int slot) {
-  if (h->timing) {
-    cudaEventRecord(h->ev[slot], h->stream);
-    h->tmask |= 1u << slot;
-  }
-}
-
 // reads the device status word; FEM_ERR_CHOLESKY if a factorisation failed
 int sync_status(fem_em *h) {
   FEM_CUDA(cudaMemcpyAsync(h->hstat, h->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
   FEM_CUDA(cudaStreamSynchronize(h->stream));
   if (h->timing) {
     float ms = 0;
-    double *acc[3] = {&h->t_estep, &h->t_mstep, &h->t_final};
-    for (int p = 0; p < 3; p++) {
+    double *acc[5] = {&h->t_estep, &h->t_mstep, &h->t_final, nullptr, &h->t_cov};
+    for (int p = 0; p < 5; p++) {
       const unsigned both = 3u << (2 * p);
-      if ((h->tmask & both) == both &&
+      if (acc[p] && (h->tmask & both) == both &&
           cudaEventElapsedTime(&ms, h->ev[2 * p], h->ev[2 * p + 1]) == cudaSuccess)
         *acc[p] += ms;
     }
@@ -495,7 +495,7 @@ int fem_em_get_factors(fem_em *h, double *U, double *logdet) {
 int fem_em_timing_reset(fem_em *h, int enable) {
   FEM_TRY(check_handle(h));
   h->timing = enable != 0;
-  h->t_estep = h->t_mstep = h->t_final = h->t_train = 0.0;
+  h->t_estep = h->t_mstep = h->t_final = h->t_train = h->t_cov = 0.0;
   h->launches = h->sweeps = 0;
   return FEM_OK;
 }
@@ -504,6 +504,12 @@ int fem_em_timing_total(fem_em *h, double *train_ms, int64_t *sweeps) {
   FEM_TRY(check_handle(h));
   if (train_ms) *train_ms = h->t_train;
   if (sweeps) *sweeps = h->sweeps;
+  return FEM_OK;
+}
+
+int fem_em_timing_covariance(fem_em *h, double *cov_ms) {
+  FEM_TRY(check_handle(h));
+  if (cov_ms) *cov_ms = h->t_cov;
   return FEM_OK;
 }
 

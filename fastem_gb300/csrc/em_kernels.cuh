@@ -22,6 +22,8 @@ int em_tc_upload(fem_em *h);    // X -> bf16 hi/lo split
 int em_tc_prepare(fem_em *h);   // factors -> permuted bf16 hi/lo operands + offsets
 int em_tc_estep(fem_em *h);
 int em_tc_mstep(fem_em *h);
+// records event `slot` on the handle's stream when timing is enabled
+void timing_begin(fem_em *h, int slot);
 int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);
 int em_tc_classes(fem_em *h, int32_t *dcls);
 

@@ -989,9 +989,11 @@ int em_tc_mstep(fem_em *h) {
   FEM_CUDA(cudaGetLastError());
   const int64_t nblocks = (h->n + kBlk - 1) / kBlk;
   const int64_t bpc = (nblocks + p->cgy - 1) / p->cgy;
+  timing_begin(h, 8);
   k_cov_tc<<<dim3(p->cgx, p->cgy), kCThreads, csmem_bytes(), h->stream>>>(p->tm_x32, p->tm_rh4, p->tm_rl4, p->muf,
                                                                          h->n, bpc, p->cpart, p->dpart, p->err);
   FEM_CUDA(cudaGetLastError());
+  timing_begin(h, 9);
   k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->psum, h->sigma);
   FEM_CUDA(cudaGetLastError());
   k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);

@@ -125,8 +125,8 @@ struct fem_em {
   // timing
   bool timing = false;
   unsigned tmask = 0;            // event slots recorded since the last sync
-  cudaEvent_t ev[8] = {};
-  double t_estep = 0, t_mstep = 0, t_final = 0, t_train = 0;
+  cudaEvent_t ev[10] = {};       // 0/1 E-step, 2/3 M-step, 4/5 factorisation, 6/7 train, 8/9 covariance kernel
+  double t_estep = 0, t_mstep = 0, t_final = 0, t_train = 0, t_cov = 0;
   int64_t launches = 0, sweeps = 0;
 };
 

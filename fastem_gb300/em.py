@@ -188,5 +188,7 @@ class CudaMatrixEM:
                                           ctypes.byref(f), ctypes.byref(n)))
         t, sw = ctypes.c_double(), ctypes.c_int64()
         C.check(C.lib().fem_em_timing_total(self._h, ctypes.byref(t), ctypes.byref(sw)))
+        cov = ctypes.c_double()
+        C.check(C.lib().fem_em_timing_covariance(self._h, ctypes.byref(cov)))
         return dict(estep_ms=e.value, mstep_ms=m.value, factor_ms=f.value, launches=n.value,
-                    train_ms=t.value, sweeps=sw.value)
+                    train_ms=t.value, sweeps=sw.value, cov_ms=cov.value)

@@ -135,6 +135,9 @@ int fem_em_timing_get(fem_em *h, double *estep_ms, double *mstep_ms, double *fin
 /* device time (ms) from the first to the last kernel of every
  * fem_em_train sweep loop since the last reset, and the sweeps it ran */
 int fem_em_timing_total(fem_em *h, double *train_ms, int64_t *sweeps);
+/* device time (ms) of the mixed-precision covariance kernel alone (the
+ * rank-update part of EM2/MatrixEM.cpp:90-99) since the last reset */
+int fem_em_timing_covariance(fem_em *h, double *cov_ms);
 
 /* ============================== k-means ============================== */
 
