@@ -35,6 +35,7 @@ EXPORTS = [
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
+    "fem_km_classify_noalloc",
 ]
 
 
@@ -111,6 +112,7 @@ def lib():
         "fem_km_get_assignment": ([P, P], i32),
         "fem_km_seed": ([P, ctypes.c_uint64], i32),
         "fem_km_stats": ([P, P, P, P], i32),
+        "fem_km_classify_noalloc": ([i32, i64, i32, P, P, P, P, i32, P], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -173,6 +173,23 @@ int fem_km_run(fem_km *h, double *centroids, double min_rel, int max_iter, doubl
 int fem_km_get_assignment(fem_km *h, int32_t *labels);
 /* reseed the repair RNG (SRand, Util/Rand.cpp:33-35) */
 int fem_km_seed(fem_km *h, uint64_t seed);
+
+/* k-means classification that allocates nothing.  No counterpart in the
+ * reference: a handle-free variant of the assignment kernel with the
+ * semantics of CentroidVector::ClassifyDataset + ComputeMSE
+ * (Clust/CentroidVector.cpp:8-34,56-94), for callers that must not allocate
+ * device memory once running.  dX (n x d float, row-major), dCent (k x d
+ * double), dLabels (n int32) and dFit (one double: sum of squared distances
+ * / n) are caller-owned device buffers on `device`; `stream` is a
+ * cudaStream_t (NULL: the default stream); the call is asynchronous.
+ * Scratch is one fixed 140 KiB __device__ array: k <= 1024, k*d <= 32768,
+ * d in {2,4,8,16,32,64}; larger k fail with FEM_ERR_BAD_ARG.  The first call
+ * on a device does the set-up (resolves the array's address) and should
+ * precede any stream capture.  Every call on a device shares the array: it
+ * keeps the last call's contents, nothing in it has to start at zero, and
+ * calls that overlap in time race. */
+int fem_km_classify_noalloc(int d, int64_t n, int k, const float *dX, const double *dCent,
+                            int32_t *dLabels, double *dFit, int device, void *stream);
 /* diagnostics: rows re-decided in FP64 and kernel time of the last iteration */
 int fem_km_stats(fem_km *h, int64_t *rechecked_rows, double *assign_ms, double *update_ms);
 
