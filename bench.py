@@ -6,9 +6,13 @@ the plain FP32 CUDA-core sweep, with the reference's CPU algorithm (the FP64
 oracle port, OpenMP) timed on the host cores.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --workload kmeans [...]
 
 One step = one EM sweep (E-step + M-step + regularise/factorise) over all N
 points, the body of EMAlgorithm::TrainNoCopy.  Prints one JSON line (rank 0).
+`--workload kmeans` measures one Lloyd iteration (NaiveKMA::
+ComputeMSEAndCorrect) at N = 2^24, d = 32, K = 256 instead (not the headline
+metric; its roofline is HBM bandwidth).
 Multi-GPU runs are independent replicas (the reference's data-parallel MPI
 path is not part of this backend): value = all sweeps of all ranks / max time.
 """
@@ -39,7 +43,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=1 << 23)
+    ap.add_argument("--workload", default="em", choices=["em", "kmeans"])
+    ap.add_argument("--n", type=int, default=None, help="points (default 2^23 EM, 2^24 k-means)")
     ap.add_argument("--k", type=int, default=128)
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core comparison")
     ap.add_argument("--no-e2e", action="store_true")
@@ -227,6 +232,13 @@ def run_reference(args, rank, world):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "kmeans":
+        if args.n is None:
+            args.n = 1 << 24
+        run_kmeans(args, rank, world, local)
+        return
+    if args.n is None:
+        args.n = 1 << 23
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -334,6 +346,146 @@ def main():
         "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
+
+
+KM_METRIC = "k-means iter/s N=2^24 d=32 K=256 (labels bit-exact to FP64)"
+KM_PROFILE_FILE = os.path.join(ROOT, "profiles", "kmeans_assign_n16m_d32_k256.md")
+
+
+def km_workload(n, d, k):
+    from fastem_gb300 import synth
+    X, _ = synth.kmeans_blobs(seed=2, n=n, d=d, k=k)
+    C0 = synth.dsquared_init(X, k, seed=3)[1].copy()
+    return X, C0
+
+
+def time_km_iterations(km, C, warmup, steps, dist):
+    """Device time (library CUDA events: assignment + update kernels) of
+    `steps` Lloyd iterations after `warmup`."""
+    for _ in range(warmup):
+        km.ComputeMSEAndCorrect(C)
+    dist.barrier()
+    a = u = 0.0
+    launches = 0
+    for _ in range(steps):
+        km.ComputeMSEAndCorrect(C)
+        st = km.Stats()
+        a += st["assign_ms"]
+        u += st["update_ms"]
+        launches += 4 if km.precision == "mixed" else 3
+    dist.barrier()
+    return a, u, launches, st["rechecked"]
+
+
+def run_kmeans(args, rank, world, local):
+    """Lloyd k-means at N = 2^24, d = 32, K = 256 (equal isotropic blobs,
+    sigma 1, centres U[-20, 20]^32; D^2-sampled initial centroids): mixed
+    (tcgen05 GEMM + argmin, FP32 refinement, FP64 recheck) against the FP32
+    CUDA-core path; roofline = HBM (read X once, write labels)."""
+    import torch
+    from fastem_gb300 import CudaKMA
+    n, d, k = args.n, 32, 256
+    if args.impl == "reference":
+        if rank == 0:
+            X, C0 = km_workload(n, d, k)
+            cpu = km_cpu_baseline(X, C0)
+            print(json.dumps({"metric": KM_METRIC, "impl": "reference", "value": cpu["value"], "unit": UNIT,
+                              "n_gpus": world, "steps": 1, "warmup": 1, "higher_is_better": True,
+                              "cpu_baseline": cpu, "e2e": {"value": cpu["value"], "unit": UNIT,
+                                                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                              "config": {"workload": "kmeans_blobs N=%d d=%d K=%d" % (n, d, k)}}), flush=True)
+        return
+    dist = Dist(world)
+    torch.cuda.set_device(local)
+    X, C0 = km_workload(n, d, k)
+    algo_bytes = n * d * 4 + n * 4
+    with CudaKMA(d, n, k, precision="mixed", device=local, repair=True) as km:
+        km.SetDataset(X)
+        km.InitDataStructures()
+        C = C0.copy()
+        clocks = Clocks(local)
+        clocks.start()
+        a, u, launches, rech = time_km_iterations(km, C, args.warmup, args.steps, dist)
+        clk = clocks.stop()
+        ms = dist.max(a + u) / args.steps
+        assign_ms = a / args.steps
+        # end to end through the C-ABI: dataset upload from pinned host memory + one iteration
+        e2e = None
+        if not args.no_e2e:
+            hostX = torch.from_numpy(X).pin_memory()
+            from fastem_gb300 import _capi as Cc
+            steps = max(1, min(args.steps, 5))
+            Ce = C0.copy()
+            dist.barrier()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                Cc.check(Cc.lib().fem_km_upload(km.handle, ctypes.c_void_p(hostX.data_ptr()), d))
+                km.ComputeMSEAndCorrect(Ce)
+            dt = dist.max(time.perf_counter() - t0)
+            e2e = {"value": world * steps / dt, "unit": UNIT, "h2d_bytes_per_step": n * d * 4 + k * d * 8,
+                   "d2h_bytes_per_step": (k * d + 2 * k) * 8}
+    value = world * 1e3 / ms
+    fp32 = None
+    if not args.no_fp32:
+        with CudaKMA(d, n, k, precision="fp32", device=local, repair=True) as k32:
+            k32.SetDataset(X)
+            k32.InitDataStructures()
+            C32 = C0.copy()
+            a32, u32, _, r32 = time_km_iterations(k32, C32, 1, max(2, args.steps // 3), dist)
+            ms32 = dist.max(a32 + u32) / max(2, args.steps // 3)
+            fp32 = {"value": world * 1e3 / ms32, "ms_per_step": ms32, "rechecked_rows": r32}
+    cpu = km_cpu_baseline(X, C0) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    dist.close()
+    if rank != 0:
+        return
+    peak = None
+    try:
+        with open(PEAKS_FILE) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        src = "measured (MEASURED_PEAKS hbm_gbs)"
+    except Exception:
+        peak, src = 6800.0, "fallback 6.8 TB/s"
+    achieved = algo_bytes / (assign_ms / 1e3) / 1e9
+    traffic = None
+    try:
+        for line in open(KM_PROFILE_FILE):
+            if line.startswith("traffic_bytes_per_launch k_km_assign_tc"):
+                traffic = float(line.split("=")[-1])
+    except OSError:
+        pass
+    line = {
+        "metric": KM_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp16x3 distances, fp32 refinement, fp64 recheck",
+        "data": "synthetic kmeans_blobs (seeded; equal isotropic blobs, sigma 1, centres U[-20,20]^32)",
+        "config": {"workload": "kmeans_blobs N=%d d=%d K=%d, one Lloyd iteration per step" % (n, d, k),
+                   "n": n, "d": d, "k": k, "init": "D^2 sampling on a 65536-row sample (seed 3)",
+                   "l2": "inputs larger than L2 (X 2.1 GB)"},
+        "roofline": {"kernel": "k_km_assign_tc", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": assign_ms},
+        "rechecked_rows_last_step": rech, "e2e": e2e, "fp32_plain": fp32,
+        "speedup_vs_fp32_plain": (value / fp32["value"]) if fp32 else None,
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def km_cpu_baseline(X, C0):
+    """The oracle's Lloyd iteration (FP64, OpenMP, all host cores) on the
+    first 2^20 rows, scaled to N."""
+    from oracle import oracle as O
+    O.lib()
+    n = len(X)
+    sample = min(n, 1 << 20)
+    threads = os.cpu_count() or 1
+    Xs = np.ascontiguousarray(X[:sample])
+    O.km_iterate(Xs[:4096], C0.copy(), repair=False, nthreads=threads)
+    t0 = time.perf_counter()
+    O.km_iterate(Xs, C0.copy(), repair=False, nthreads=threads)
+    dt = (time.perf_counter() - t0) * n / sample
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "1 FP64 iteration over the first %d of %d rows, scaled x%d" % (sample, n, n // sample)}
 
 
 if __name__ == "__main__":

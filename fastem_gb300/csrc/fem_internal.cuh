@@ -160,4 +160,5 @@ struct fem_km {
   fem::DevStatus *hstat = nullptr;
   cudaEvent_t ev[4] = {};
   double t_assign = 0, t_update = 0;
+  void *tc = nullptr;              // tensor-core plan (km_tc.cu)
 };

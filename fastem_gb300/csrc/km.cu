@@ -424,7 +424,7 @@ int fem_km_create(int d, int64_t n, int k, const fem_km_config *cfg, fem_km **ou
     return FEM_ERR_UNSUPPORTED;
   }
   if (c.precision == FEM_PREC_MIXED && !km_tc_supported(d, k)) {
-    set_error("k-means mixed path supports d in {16,32,64} and k in [16,256] multiple of 16");
+    set_error("k-means mixed (tensor-core) path supports d = 32 and k <= 256 (got d=%d k=%d)", d, k);
     return FEM_ERR_UNSUPPORTED;
   }
   if (km_assign_smem(k, d) > 220 * 1024 && c.precision == FEM_PREC_FP32) {
@@ -520,6 +520,10 @@ int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, in
   FEM_CUDA(cudaMemcpyAsync(h->hout, h->out, (kd + 2 * K) * 8, cudaMemcpyDeviceToHost, h->stream));
   FEM_CUDA(cudaMemcpyAsync(h->hstat, h->dstat, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream));
   FEM_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->hstat->timeout) {
+    set_error("a bounded device wait timed out in the tensor-core k-means kernel");
+    return FEM_ERR_TIMEOUT;
+  }
   float a = 0, b = 0;
   cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
   cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);

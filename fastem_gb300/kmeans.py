@@ -26,7 +26,12 @@ class CudaKMA:
                                       ctypes.byref(h)))
         self._h = h
         self.ncols, self.nrows, self.nclusters = int(ncols), int(nrows), int(nclusters)
+        self.precision = precision
         self.IterCount = 0
+
+    @property
+    def handle(self):
+        return self._h
 
     def close(self):
         if getattr(self, "_h", None):

@@ -36,7 +36,7 @@ def check_iters(out):
         np.testing.assert_allclose(Cg, Co, rtol=1e-13, atol=1e-13)
 
 
-@pytest.mark.parametrize("precision", ["fp32"])
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
 def test_km_blobs_30_iterations(gpu_lib, oracle, precision):
     """kmeans_blobs shape at reduced N (d=32, K=64), k-means|| seed 3, 30 iterations."""
     X, _ = synth.kmeans_blobs(seed=2, n=1 << 17, d=32, k=64)
@@ -98,3 +98,47 @@ def test_km_run_matches_oracle(gpu_lib, oracle):
         assert km.IterCount == it_o
     assert abs(best_g - best_o) <= 1e-11 * best_o
     np.testing.assert_allclose(Cg, Co, rtol=1e-13, atol=1e-13)
+
+
+# ---------------------------------------------------------------- tensor-core path (d = 32)
+
+@pytest.mark.parametrize("n,k", [(1, 5), (127, 5), (129, 17), (10001, 200), (1 << 16, 256)])
+def test_km_tc_ragged_and_padded_k(gpu_lib, oracle, n, k):
+    """Rows past N (partial 128-row tiles) and K not a multiple of 16 / 32
+    (padded MMA columns) are ignored; labels bit-exact to the oracle."""
+    X, _ = synth.kmeans_blobs(seed=9, n=max(n, k), d=32, k=k)
+    X = X[:n]
+    rng = np.random.default_rng(3)
+    C0 = X[rng.integers(0, n, size=k)].astype(np.float64) + rng.standard_normal((k, 32))
+    check_iters(iterate_both(oracle, X, C0, 3, "mixed", repair=False))
+
+
+def test_km_tc_duplicate_centroids_recheck(gpu_lib, oracle):
+    """Exact ties (a centroid repeated) cannot be separated by the bound: the
+    rows are re-decided in FP64 and the lowest index wins."""
+    X, _ = synth.kmeans_blobs(seed=10, n=20000, d=32, k=16)
+    C0 = oracle.kmeans_forgy(X, 16, seed=2)
+    C0[9] = C0[3]
+    C0[15] = C0[3]
+    with CudaKMA(32, len(X), 16, precision="mixed", repair=False) as km:
+        km.SetDataset(X)
+        C = C0.copy()
+        km.ComputeMSEAndCorrect(C)
+        lg = km.Assignment()
+        st = km.Stats()
+    fo, Co, co, lo = oracle.km_iterate(X, C0.copy(), repair=False)
+    assert np.array_equal(lg, lo)
+    assert (lg == 9).sum() == 0 and (lg == 15).sum() == 0
+    assert st["rechecked"] >= (lo == 3).sum()
+    np.testing.assert_allclose(C, Co, rtol=1e-13, atol=1e-13)
+
+
+def test_km_tc_far_from_origin(gpu_lib, oracle):
+    """Blobs offset by 3e3 (||x|| ~ 2e4, so the error of ||c||^2 - 2 x.c grows
+    with ||x|| ||c||): the bound must still hold; labels bit-exact."""
+    X, _ = synth.kmeans_blobs(seed=12, n=1 << 16, d=32, k=64, spread=20.0, sigma=1.0)
+    X = (X + 3000.0).astype(np.float32)
+    C0 = oracle.kmeans_forgy(X, 64, seed=4)
+    out = iterate_both(oracle, X, C0, 4, "mixed", repair=False)
+    check_iters(out)
+    print("rechecked rows per iteration:", [o[-1]["rechecked"] for o in out])
