@@ -96,7 +96,7 @@ struct __align__(1024) MSmem {
 
 // covariance kernel: 4 components per CTA (2 pairs), 64-point blocks
 constexpr int kZStages = 3;              // operand (z) ring
-constexpr int kCProd = 16;               // producer warps: 2 dimension halves x 8 point chunks
+constexpr int kCProd = 16;               // producer warps: 2 groups x 8 point chunks
 struct __align__(1024) CSmem {
   __half z[kZStages][2][128 * kBlk];  // [stage][pair] 128 rows (comp q dims) x 64 points, SW128
   float xs[kCIn][kBlk * kD];     // X tile (points x dims)
@@ -519,10 +519,13 @@ __global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, 
 
 // ========================================================= covariances
 // CTA (blockIdx.x = group of 4 components, blockIdx.y = chunk of points).
-// Producer thread (warps 2..17): dimension a, 8-point chunk c8; for each of
-// the 4 components q it writes z = sqrt(r) (x - mu) of its 8 points as one
-// 16-byte store into row (q % 2) * 64 + a of pair q / 2's operand tile
-// (128-byte swizzle) and sums z^2 in FP32 / FP64 for the exact diagonal.
+// Producers (warps 2..17) form two groups of eight that take alternate
+// blocks.  Warp c8 of a group owns the block's points 8 c8 .. 8 c8 + 7; lane a
+// owns dimensions a and a + 32 (32 apart, so the eight rows a phase of a
+// 16-byte store touches fall in eight different swizzle chunks).  For each of
+// the 4 components q a thread writes z = sqrt(r) (x - mu) of its 8 points as
+// one 16-byte store into rows (q % 2) * 64 + a (+ 32) of pair q / 2's operand
+// tile and sums z^2 in FP32 / FP64 for the exact diagonal.
 __global__ void __launch_bounds__(kCThreads, 1)
 k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUtensorMap tm_rh4,
          const __grid_constant__ CUtensorMap tm_rl4, const float *__restrict__ muf, int64_t n,
@@ -530,7 +533,7 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
   extern __shared__ uint8_t smem_raw[];
   CSmem &S = smem_aligned<CSmem>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int grp = blockIdx.x;
+  const int cg = blockIdx.x;                  // component group (4 components)
   const int64_t nblocks = (n + kBlk - 1) / kBlk;
   const int64_t b0 = (int64_t)blockIdx.y * blocks_per_chunk;
   const int64_t mine = std::max<int64_t>(0, std::min<int64_t>(nblocks, b0 + blocks_per_chunk) - b0);
@@ -538,8 +541,9 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
   const size_t cta = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kCIn; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], kCProd);
-    for (int s = 0; s < kZStages; s++) mbar_init(&S.z_full[s], kCProd), mbar_init(&S.z_empty[s], 1);
+    // each block is produced by one group of kCProd / 2 warps
+    for (int s = 0; s < kCIn; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.in_empty[s], kCProd / 2);
+    for (int s = 0; s < kZStages; s++) mbar_init(&S.z_full[s], kCProd / 2), mbar_init(&S.z_empty[s], 1);
     for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
@@ -560,8 +564,8 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         const int p0 = (int)((b0 + t) * kBlk);
         mbar_expect_tx(&S.in_full[s], kInBytes);
         tma_load_2d(S.xs[s], &tm_x32, &S.in_full[s], 0, p0);
-        tma_load_2d(S.rh[s], &tm_rh4, &S.in_full[s], p0, grp * 4);
-        tma_load_2d(S.rl[s], &tm_rl4, &S.in_full[s], p0, grp * 4);
+        tma_load_2d(S.rh[s], &tm_rh4, &S.in_full[s], p0, cg * 4);
+        tma_load_2d(S.rl[s], &tm_rl4, &S.in_full[s], p0, cg * 4);
       }
       for (int64_t u = mine - 1; u >= 0 && u >= mine - kCIn; u--)
         mbar_wait_drain(&S.in_full[u % kCIn], (u / kCIn) & 1);
@@ -596,25 +600,26 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     }
   } else if (warp < 2 + kCProd) {
     // ------------------------------------------------ producers
-    // thread t: dimension a = t % 64 and the 8-point chunk c8 = t / 64 of
-    // the block, for all 4 components (x is read once per point). Each warp
-    // computes sqrt(r) of its own 8 points x 4 components (one per lane)
-    // into its own slot, so producers synchronise only through mbarriers.
-    const int t = threadIdx.x - 64;             // 0..511
-    const int a = t & 63, c8 = t >> 6;
-    float *srw = S.sr[warp - 2];
-    float2 nmu[4];
+    const int pw = warp - 2, grp = pw >> 3, c8 = pw & 7;
+    const int a = lane;                          // dimensions a and a + 32
+    float *srw = S.sr[pw];
+    float2 nmu[4][2];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const float m = muf[(size_t)(grp * 4 + q) * kD + a];
-      nmu[q] = make_float2(-m, -m);
-    }
-    double diag[4] = {0.0, 0.0, 0.0, 0.0};
-    float2 dwin[4];
+    for (int q = 0; q < 4; q++)
 #pragma unroll
-    for (int q = 0; q < 4; q++) dwin[q] = make_float2(0.f, 0.f);
+      for (int h = 0; h < 2; h++) {
+        const float m = muf[(size_t)(cg * 4 + q) * kD + a + 32 * h];
+        nmu[q][h] = make_float2(-m, -m);
+      }
+    double diag[4][2];
+    float2 dwin[4][2];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int h = 0; h < 2; h++) diag[q][h] = 0.0, dwin[q][h] = make_float2(0.f, 0.f);
     bool ok = true;
-    for (int64_t tb = 0; tb < mine && ok; tb++) {
+    int li = 0;                                  // blocks this group has produced
+    for (int64_t tb = grp; tb < mine && ok; tb += 2, li++) {
       const int si = (int)(tb % kCIn), sz = (int)(tb % kZStages);
       if (!(ok = mbar_wait_warp(&S.in_full[si], (tb / kCIn) & 1, err))) break;
       {
@@ -628,9 +633,11 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         __syncwarp();
       }
       const float *xr = S.xs[si] + (c8 * 8) * kD + a;
-      float2 xv[4];
+      float2 xv[2][4];                           // [dimension a / a + 32][point pair]
 #pragma unroll
-      for (int u = 0; u < 4; u++) xv[u] = make_float2(xr[(2 * u) * kD], xr[(2 * u + 1) * kD]);
+      for (int h = 0; h < 2; h++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) xv[h][u] = make_float2(xr[(2 * u) * kD + 32 * h], xr[(2 * u + 1) * kD + 32 * h]);
       if (!(ok = mbar_wait_warp(&S.z_empty[sz], ((tb / kZStages) & 1) ^ 1, err))) break;
 #pragma unroll
       for (int q = 0; q < 4; q++) {
@@ -638,17 +645,20 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         const float4 s1 = *reinterpret_cast<const float4 *>(srw + q * 8 + 4);
         const float2 s2[4] = {make_float2(s0.x, s0.y), make_float2(s0.z, s0.w), make_float2(s1.x, s1.y),
                               make_float2(s1.z, s1.w)};
-        uint32_t w4[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const float2 z = __fmul2_rn(__fadd2_rn(xv[u], nmu[q]), s2[u]);
-          dwin[q] = __ffma2_rn(z, z, dwin[q]);
-          const __half2 hz = __floats2half2_rn(z.x, z.y);
-          w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+        for (int h = 0; h < 2; h++) {
+          uint32_t w4[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const float2 z = __fmul2_rn(__fadd2_rn(xv[h][u], nmu[q][h]), s2[u]);
+            dwin[q][h] = __ffma2_rn(z, z, dwin[q][h]);
+            const __half2 hz = __floats2half2_rn(z.x, z.y);
+            w4[u] = *reinterpret_cast<const uint32_t *>(&hz);
+          }
+          const int row = ((q & 1) << 6) + a + 32 * h;
+          uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
+          *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
         }
-        const int row = ((q & 1) << 6) + a;
-        uint8_t *zrow = reinterpret_cast<uint8_t *>(S.z[sz][q >> 1]) + row * 128;
-        *reinterpret_cast<uint4 *>(zrow + ((c8 ^ (row & 7)) << 4)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
       }
       fence_proxy_async_smem();
       __syncwarp();
@@ -656,24 +666,40 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
         mbar_arrive(&S.z_full[sz]);
         mbar_arrive(&S.in_empty[si]);
       }
-      if ((tb + 1) % kFlushBlocks == 0) {
+      if ((li + 1) % (kFlushBlocks / 2) == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q].x + (double)dwin[q].y, dwin[q] = make_float2(0.f, 0.f);
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+            diag[q][h] += (double)dwin[q][h].x + (double)dwin[q][h].y, dwin[q][h] = make_float2(0.f, 0.f);
       }
     }
 #pragma unroll
-    for (int q = 0; q < 4; q++) diag[q] += (double)dwin[q].x + (double)dwin[q].y;
-    // exact diagonal: combine the 8 point chunks in a fixed order
+    for (int q = 0; q < 4; q++)
 #pragma unroll
-    for (int q = 0; q < 4; q++) S.dred[c8][q][a] = diag[q];
+      for (int h = 0; h < 2; h++) diag[q][h] += (double)dwin[q][h].x + (double)dwin[q][h].y;
+    // exact diagonal: group 0, then group 1 added, then the 8 point chunks in order
+    if (grp == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) S.dred[c8][q][a + 32 * h] = diag[q][h];
     asm volatile("bar.sync 2, %0;" ::"n"(kCProd * 32) : "memory");
-    if (c8 == 0)
+    if (grp == 1)
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        double v = S.dred[0][q][a];
-        for (int c = 1; c < 8; c++) v += S.dred[c][q][a];
-        dpart[(cta * 4 + q) * kD + a] = v;
-      }
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) S.dred[c8][q][a + 32 * h] += diag[q][h];
+    asm volatile("bar.sync 2, %0;" ::"n"(kCProd * 32) : "memory");
+    if (grp == 0 && c8 == 0)
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          double v = S.dred[0][q][a + 32 * h];
+          for (int c = 1; c < 8; c++) v += S.dred[c][q][a + 32 * h];
+          dpart[(cta * 4 + q) * kD + a + 32 * h] = v;
+        }
   } else {
     // ------------------------------------------------ flush warps 18..21
     const int quad = warp & 3;
