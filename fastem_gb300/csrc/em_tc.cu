@@ -77,7 +77,7 @@ struct __align__(1024) ESmem {
   float chi[kMaxK], clo[kMaxK];
   uint64_t x_full, x_empty;
   uint64_t w_full[kWStages], w_empty[kWStages];
-  uint64_t acc_full[2], acc_empty[2];
+  uint64_t acc_full[2][2], acc_empty[2][2];   // [TMEM buffer][tile of the pair]
   uint64_t mma_done;
   uint32_t tmem_base;
   double red[8];
@@ -160,7 +160,8 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
   if (threadIdx.x == 0) {
     mbar_init(&S.x_full, 1), mbar_init(&S.x_empty, 1);
     for (int s = 0; s < kWStages; s++) mbar_init(&S.w_full[s], 1), mbar_init(&S.w_empty[s], 1);
-    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 8);
+    for (int s = 0; s < 2; s++)
+      for (int t = 0; t < 2; t++) mbar_init(&S.acc_full[s][t], 1), mbar_init(&S.acc_empty[s][t], 4);
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
   }
@@ -222,29 +223,35 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
         }
         for (int g = 0; g < G; g++) {
           const int ws = wi % kWStages, ab = ai & 1;
-          if (!(ok = mbar_wait(&S.acc_empty[ab], ((ai >> 1) & 1) ^ 1, err))) break;
           if (!(ok = mbar_wait(&S.w_full[ws], (wi / kWStages) & 1, err))) break;
-          tc_fence_after();
           const uint64_t dwh = sdesc_sw128(smem_u32(S.wh[ws]));
           const uint64_t dwl = sdesc_sw128(smem_u32(S.wl[ws]));
-          for (int t = 0; t < nt; t++) {
-            const uint32_t dt = tbase + (2 * ab + t) * kGroupN;
-            // the small cross products Xh Wl and Xl Wh first, Xh Wh last: the
-            // accumulator is rounded after every MMA, and it only grows to
-            // |W x| during the final four steps
+          // each tile has its own accumulator barriers, so its epilogue warps
+          // start as soon as its own products are done; a pair with one tile
+          // still completes the second tile's phases (no products)
+          for (int t = 0; t < 2; t++) {
+            if (!(ok = mbar_wait(&S.acc_empty[ab][t], ((ai >> 1) & 1) ^ 1, err))) break;
+            tc_fence_after();
+            if (t < nt) {
+              const uint32_t dt = tbase + (2 * ab + t) * kGroupN;
+              // the small cross products Xh Wl and Xl Wh first, Xh Wh last: the
+              // accumulator is rounded after every MMA, and it only grows to
+              // |W x| during the final four steps
 #pragma unroll
-            for (int p = 0; p < 3; p++) {
-              const uint64_t da = (p == 1) ? dxl[t] : dxh[t];
-              const uint64_t db = (p == 0) ? dwl : dwh;
+              for (int p = 0; p < 3; p++) {
+                const uint64_t da = (p == 1) ? dxl[t] : dxh[t];
+                const uint64_t db = (p == 0) ? dwl : dwh;
 #pragma unroll
-              for (int kb = 0; kb < kD / 16; kb++) {
-                // +32 bytes per 16-element K step inside the 128-byte swizzle row
-                mma_f16(dt, da + 2 * kb, db + 2 * kb, idesc_f16(kTileM, kGroupN - 32 * kb), (p | kb) != 0);
+                for (int kb = 0; kb < kD / 16; kb++) {
+                  // +32 bytes per 16-element K step inside the 128-byte swizzle row
+                  mma_f16(dt, da + 2 * kb, db + 2 * kb, idesc_f16(kTileM, kGroupN - 32 * kb), (p | kb) != 0);
+                }
               }
             }
+            mma_commit(&S.acc_full[ab][t]);
           }
+          if (!ok) break;
           mma_commit(&S.w_empty[ws]);
-          mma_commit(&S.acc_full[ab]);
           wi++;
           ai++;
         }
@@ -288,34 +295,39 @@ k_estep_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CU
           for (int q = 0; q < 2; q++) lp[q] = scr[(size_t)(prev_par * K + 2 * g + q) * (2 * kTileM)];
         }
         const int ab = ai & 1;
-        if (!(ok = mbar_wait_warp(&S.acc_full[ab], (ai >> 1) & 1, err))) break;
+        if (!(ok = mbar_wait_warp(&S.acc_full[ab][tile], (ai >> 1) & 1, err))) break;
         tc_fence_after();
         float s[kCompPerGroup] = {0.f, 0.f};
         if (live) {
           const float *bg = S.bias + g * kGroupN;
           // 32-column block bp holds k-block (3 - bp) of both components:
-          // column 32 bp + 16 q + t belongs to component q
+          // column 32 bp + 16 q + t belongs to component q; two 64-column
+          // loads per group, column pairs in packed FP32 arithmetic
+          float2 s2[kCompPerGroup] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll 1
-          for (int bp = 0; bp < kGroupN / 32; bp++) {
-            uint32_t v[32];
-            tmem_ld32(tbase + lane_addr + (2 * ab + tile) * kGroupN + bp * 32, v);
-            float4 b[8];
-            const float4 *b4 = reinterpret_cast<const float4 *>(bg + bp * 32);
-#pragma unroll
-            for (int u = 0; u < 8; u++) b[u] = b4[u];
+          for (int hp = 0; hp < kGroupN / 64; hp++) {
+            uint32_t v[64];
+            tmem_ld64(tbase + lane_addr + (2 * ab + tile) * kGroupN + hp * 64, v);
             tmem_wait_ld();
+            const float4 *b4 = reinterpret_cast<const float4 *>(bg + hp * 64);
 #pragma unroll
-            for (int t = 0; t < 32; t++) {
-              const float bb = (t & 3) == 0 ? b[t >> 2].x : (t & 3) == 1 ? b[t >> 2].y
-                             : (t & 3) == 2 ? b[t >> 2].z : b[t >> 2].w;
-              const float y = __uint_as_float(v[t]) - bb;
-              s[t >> 4] = fmaf(y, y, s[t >> 4]);
+            for (int u = 0; u < 16; u++) {
+              const float4 b = b4[u];
+              const int q = (u >> 2) & 1;         // columns 4u .. 4u + 3
+              const float2 y0 = __fadd2_rn(make_float2(__uint_as_float(v[4 * u]), __uint_as_float(v[4 * u + 1])),
+                                           make_float2(-b.x, -b.y));
+              const float2 y1 = __fadd2_rn(make_float2(__uint_as_float(v[4 * u + 2]), __uint_as_float(v[4 * u + 3])),
+                                           make_float2(-b.z, -b.w));
+              s2[q] = __ffma2_rn(y0, y0, s2[q]);
+              s2[q] = __ffma2_rn(y1, y1, s2[q]);
             }
           }
+          s[0] = s2[0].x + s2[0].y;
+          s[1] = s2[1].x + s2[1].y;
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
+        if (lane == 0) mbar_arrive(&S.acc_empty[ab][tile]);
         ai++;
         if (have_prev && prev_i >= 0) {
 #pragma unroll
