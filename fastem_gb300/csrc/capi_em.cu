@@ -172,8 +172,8 @@ int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **ou
     return FEM_ERR_BAD_ARG;
   }
   if (c.precision == FEM_PREC_MIXED && !em_tc_supported(d, k)) {
-    set_error("mixed precision (tensor-core kernels) needs d = 64, k a multiple of 4 and k <= 128 "
-              "(got d=%d k=%d); use FEM_PREC_FP32 or FEM_PREC_FP64", d, k);
+    set_error("mixed precision (tensor-core kernels) needs d <= 64 and k <= 128 (got d=%d k=%d); "
+              "use FEM_PREC_FP32 or FEM_PREC_FP64", d, k);
     return FEM_ERR_UNSUPPORTED;
   }
   FEM_TRY(select_device(c.device));

@@ -22,6 +22,8 @@ int em_tc_upload(fem_em *h);    // X -> bf16 hi/lo split
 int em_tc_prepare(fem_em *h);   // factors -> permuted bf16 hi/lo operands + offsets
 int em_tc_estep(fem_em *h);
 int em_tc_mstep(fem_em *h);
+// device posteriors of the mixed path: FP16 hi / lo, component-major, row pitch
+void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch);
 // records event `slot` on the handle's stream when timing is enabled
 void timing_begin(fem_em *h, int slot);
 int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);

@@ -127,8 +127,11 @@ struct TcEmPlan {
   double *cpart = nullptr;              // covariance partials: cgrid x 4 x 64 x 64
   double *dpart = nullptr;              // exact diagonals: cgrid x 4 x 64
   float *muf = nullptr;                 // new means (float) for the covariance producers
+  float *chi = nullptr;                 // float(log coefficient); -inf for padding components
+  float *X64 = nullptr;                 // n x 64 zero-padded FP32 rows when d < 64
   int *err = nullptr;                   // device status of the bounded waits
   int egrid = 0, mgrid = 0, cgx = 0, cgy = 0;
+  int kp = 0, d = 0;                    // components padded to a multiple of 4; true dimension
 };
 
 __device__ __forceinline__ void fence_proxy_async_smem() {
@@ -507,7 +510,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
 }
 
 // S1 = sum r, mu = S2 / S1, pi = S1 / N (FP64, blocks summed in order)
-__global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, int64_t n,
+__global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, int d, int64_t n,
                                  double *__restrict__ mu, double *__restrict__ pi,
                                  double *__restrict__ psum, float *__restrict__ muf) {
   const int j = blockIdx.x;
@@ -524,8 +527,8 @@ __global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, 
     double s = 0.0;
     for (int g = 0; g < G; g++) s += part[((size_t)g * kMaxK + j) * kMeanN + q];
     const double m = s / s1;
-    mu[(size_t)j * kD + q] = m;
-    muf[(size_t)j * kD + q] = (float)m;
+    if (q < d) mu[(size_t)j * d + q] = m;
+    muf[(size_t)j * kD + q] = q < d ? (float)m : 0.f;
   }
 }
 
@@ -752,12 +755,12 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
 
 // Covs_j = sym(S3_j) / S1_j with the exact diagonal (FP64, chunks in order)
 __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *__restrict__ dpart, int gx,
-                               int gy, const double *__restrict__ psum, double *__restrict__ sigma) {
+                               int gy, int d, const double *__restrict__ psum, double *__restrict__ sigma) {
   const int j = blockIdx.x, grp = j / 4, q = j % 4;
   const double inv = 1.0 / psum[j];
-  double *Sg = sigma + (size_t)j * kD * kD;
-  for (int e = threadIdx.x; e < kD * kD; e += blockDim.x) {
-    const int a = e / kD, b = e - a * kD;
+  double *Sg = sigma + (size_t)j * d * d;
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    const int a = e / d, b = e - a * d;
     if (b < a) continue;
     double s = 0.0;
     if (a == b) {
@@ -769,8 +772,8 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
       }
     }
     s *= inv;
-    Sg[a * kD + b] = s;
-    Sg[b * kD + a] = s;
+    Sg[a * d + b] = s;
+    Sg[b * d + a] = s;
   }
 }
 
@@ -783,30 +786,40 @@ __device__ __forceinline__ int w_row(int j, int k) {
          (j % kCompPerGroup) * 16 + (k & 15);
 }
 
-__global__ void k_prep_w(const double *__restrict__ linv, const double *__restrict__ mu, int K,
+// Dimensions d..63 of a component with d < 64 get zero rows and columns
+// (x and mu are zero there, so y = 0), components K..Kp-1 (padding to a
+// multiple of 4) get W = 0 and a log coefficient of -inf (posterior 0).
+__global__ void k_prep_w(const double *__restrict__ linv, const double *__restrict__ mu, int K, int d,
                          __half *__restrict__ Wh, __half *__restrict__ Wl, float *__restrict__ bias,
-                         const double *__restrict__ logc, float *__restrict__ clo) {
+                         const double *__restrict__ logc, float *__restrict__ chi, float *__restrict__ clo) {
   const int j = blockIdx.x;
-  if (threadIdx.x == 0) clo[j] = (float)(logc[j] - (double)(float)logc[j]);
+  const bool live = j < K;
+  if (threadIdx.x == 0) {
+    chi[j] = live ? (float)logc[j] : -INFINITY;
+    clo[j] = live ? (float)(logc[j] - (double)(float)logc[j]) : 0.f;
+  }
   for (int e = threadIdx.x; e < kD * kD; e += blockDim.x) {
     const int k = e / kD, m = e - k * kD;
     const int row = w_row(j, k);
-    const double w = linv[(size_t)j * kD * kD + e];
+    const double w = (live && k < d && m < d) ? linv[((size_t)j * d + k) * d + m] : 0.0;
     const __half h = __double2half(w);
     Wh[(size_t)row * kD + m] = h;
     Wl[(size_t)row * kD + m] = __double2half(w - (double)__half2float(h));
   }
   for (int k = threadIdx.x; k < kD; k += blockDim.x) {
     double b = 0.0;
-    for (int m = 0; m <= k; m++) b += linv[(size_t)j * kD * kD + k * kD + m] * mu[(size_t)j * kD + m];
+    if (live && k < d)
+      for (int m = 0; m <= k; m++) b += linv[((size_t)j * d + k) * d + m] * mu[(size_t)j * d + m];
     bias[w_row(j, k)] = (float)b;
   }
 }
 
 // x -> xh = fp16(x), xl = fp16(x - xh), row-major and transposed (d x np)
-__global__ void k_split_x(const float *__restrict__ X, int64_t n, __half *__restrict__ Xh,
+// (rows of d < 64 values are zero-padded to 64; X64 receives the padded FP32
+// rows when it is not null)
+__global__ void k_split_x(const float *__restrict__ X, int64_t n, int d, __half *__restrict__ Xh,
                           __half *__restrict__ Xl, __half *__restrict__ XhT, __half *__restrict__ XlT,
-                          int64_t np, float *__restrict__ amax) {
+                          int64_t np, float *__restrict__ X64, float *__restrict__ amax) {
   __shared__ __half th[kD][65], tl[kD][65];
   float m = 0.f;
   const int64_t nt = (n + 63) / 64;
@@ -815,7 +828,8 @@ __global__ void k_split_x(const float *__restrict__ X, int64_t n, __half *__rest
     for (int e = threadIdx.x; e < 64 * kD; e += blockDim.x) {
       const int r = e / kD, c = e - r * kD;
       if (r0 + r < n) {
-        const float x = X[(r0 + r) * kD + c];
+        const float x = c < d ? X[(r0 + r) * d + c] : 0.f;
+        if (X64) X64[(r0 + r) * kD + c] = x;
         const __half h = __float2half_rn(x);
         const __half l = __float2half_rn(x - __half2float(h));
         Xh[(r0 + r) * kD + c] = h;
@@ -893,13 +907,16 @@ static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t ro
 }
 
 // the covariance kernel works on groups of 4 components
-bool em_tc_supported(int d, int k) { return d == kD && k % 4 == 0 && k <= kMaxK; }
+// d <= 64 (zero-padded to 64) and K <= 128 (padded to a multiple of 4)
+bool em_tc_supported(int d, int k) { return d >= 1 && d <= kD && k >= 1 && k <= kMaxK; }
 
 int em_tc_create(fem_em *h) {
   TcEmPlan *p = new TcEmPlan();
   h->tc = p;
-  const int K = h->k;
+  const int K = (h->k + 3) / 4 * 4;     // kernels see K padded to a multiple of 4
   const int64_t n = h->n;
+  p->kp = K;
+  p->d = h->d;
   p->np = (n + 63) / 64 * 64;
   const int sms = sm_count();
   FEM_TRY(dalloc(&h->Xhi, (size_t)n * kD));
@@ -913,6 +930,9 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(dalloc(&p->bias, (size_t)K * kD));
   FEM_TRY(dalloc(&p->clo, K));
   FEM_TRY(dalloc(&p->muf, (size_t)K * kD));
+  FEM_TRY(dalloc(&p->chi, K));
+  FEM_CUDA(cudaMemset(p->muf, 0, (size_t)K * kD * sizeof(float)));
+  if (h->d < kD) FEM_TRY(dalloc(&p->X64, (size_t)n * kD));
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
   const int64_t npairs = ((n + kTileM - 1) / kTileM + 1) / 2;
@@ -941,7 +961,8 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(encode_tmap_2d(&p->tm_xlt, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->XlT, (uint64_t)n, kD, kBlk, kD,
                          CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
   // covariance operands (no swizzle: read by CUDA cores)
-  FEM_TRY(encode_tmap_2d(&p->tm_x32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h->X, kD, (uint64_t)n, kD, kBlk,
+  FEM_TRY(encode_tmap_2d(&p->tm_x32, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, p->X64 ? p->X64 : h->X, kD, (uint64_t)n, kD,
+                         kBlk,
                          CU_TENSOR_MAP_SWIZZLE_NONE, 0));
   FEM_TRY(encode_tmap_2d(&p->tm_rh4, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rh, (uint64_t)n, (uint64_t)K, kBlk, 4,
                          CU_TENSOR_MAP_SWIZZLE_NONE, (uint64_t)p->np * 2));
@@ -970,6 +991,8 @@ void em_tc_destroy(fem_em *h) {
   dfree(p->cpart);
   dfree(p->dpart);
   dfree(p->muf);
+  dfree(p->chi);
+  dfree(p->X64);
   dfree(p->err);
   delete p;
   h->tc = nullptr;
@@ -981,7 +1004,7 @@ int em_tc_upload(fem_em *h) {
   FEM_TRY(dalloc(&amax, 1));
   FEM_CUDA(cudaMemsetAsync(amax, 0, sizeof(float), h->stream));
   const int blocks = (int)std::min<int64_t>(4 * sm_count(), (h->n + 63) / 64);
-  k_split_x<<<blocks, 256, 0, h->stream>>>(h->X, h->n, h->Xhi, h->Xlo, p->XhT, p->XlT, p->np, amax);
+  k_split_x<<<blocks, 256, 0, h->stream>>>(h->X, h->n, h->d, h->Xhi, h->Xlo, p->XhT, p->XlT, p->np, p->X64, amax);
   float m = 0.f;
   cudaMemcpyAsync(&m, amax, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
@@ -999,7 +1022,8 @@ int em_tc_upload(fem_em *h) {
 
 int em_tc_prepare(fem_em *h) {
   TcEmPlan *p = h->tc;
-  k_prep_w<<<h->k, 256, 0, h->stream>>>(h->linv, h->mu, h->k, p->Wh, p->Wl, p->bias, h->logc, p->clo);
+  k_prep_w<<<p->kp, 256, 0, h->stream>>>(h->linv, h->mu, h->k, h->d, p->Wh, p->Wl, p->bias, h->logc, p->chi,
+                                         p->clo);
   FEM_CUDA(cudaGetLastError());
   h->launches += 1;
   return FEM_OK;
@@ -1008,8 +1032,8 @@ int em_tc_prepare(fem_em *h) {
 int em_tc_estep(fem_em *h) {
   TcEmPlan *p = h->tc;
   k_estep_tc<<<p->egrid, kEThreads, esmem_bytes(), h->stream>>>(
-      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, (const float *)h->logcT, p->clo, h->logc, p->lsc, p->Rh, p->Rl,
-      p->np, p->epart, h->n, h->k, p->err);
+      p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, p->chi, p->clo, h->logc, p->lsc, p->Rh, p->Rl, p->np,
+      p->epart, h->n, p->kp, p->err);
   FEM_CUDA(cudaGetLastError());
   k_reduce_parts<<<1, 32, 0, h->stream>>>(p->epart, p->egrid, h->dstat, p->err);
   FEM_CUDA(cudaGetLastError());
@@ -1023,7 +1047,7 @@ int em_tc_mstep(fem_em *h) {
   k_means_tc<<<p->mgrid, 192, msmem_bytes(), h->stream>>>(p->tm_rh, p->tm_rl, p->tm_xht, p->tm_xlt, h->n,
                                                            p->mpart, p->err);
   FEM_CUDA(cudaGetLastError());
-  k_final_means_tc<<<K, 64, 0, h->stream>>>(p->mpart, p->mgrid, K, h->n, h->mu, h->pi, h->psum, p->muf);
+  k_final_means_tc<<<K, 64, 0, h->stream>>>(p->mpart, p->mgrid, K, h->d, h->n, h->mu, h->pi, h->psum, p->muf);
   FEM_CUDA(cudaGetLastError());
   const int64_t nblocks = (h->n + kBlk - 1) / kBlk;
   const int64_t bpc = (nblocks + p->cgy - 1) / p->cgy;
@@ -1032,7 +1056,7 @@ int em_tc_mstep(fem_em *h) {
                                                                          h->n, bpc, p->cpart, p->dpart, p->err);
   FEM_CUDA(cudaGetLastError());
   timing_begin(h, 9);
-  k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->psum, h->sigma);
+  k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->d, h->psum, h->sigma);
   FEM_CUDA(cudaGetLastError());
   k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
   h->launches += 5;
@@ -1045,6 +1069,12 @@ int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout) {
   k_post_rows_tc<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(p->Rh, p->Rl, p->np, h->k, r0, rows, dout);
   FEM_CUDA(cudaGetLastError());
   return FEM_OK;
+}
+
+void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch) {
+  *rh = h->tc->Rh;
+  *rl = h->tc->Rl;
+  *pitch = h->tc->np;
 }
 
 int em_tc_classes(fem_em *h, int32_t *dcls) {

@@ -171,6 +171,12 @@ class CudaMatrixEM:
         C.check(C.lib().fem_em_retrieve_classes(self._h, C.ptr(out)))
         return out
 
+    def ComputePosterriorCorrelation(self):
+        """R^T R (K x K) of the last E-step's posteriors."""
+        out = np.zeros((self.K, self.K))
+        C.check(C.lib().fem_em_posterior_correlation(self._h, C.ptr(out)))
+        return out
+
     def Factors(self):
         k, d = self.K, self.nCols
         U, ld = np.zeros((k, d, d)), np.zeros(k)

@@ -122,6 +122,10 @@ int fem_em_max_condition(fem_em *h, double *cond);
 int fem_em_get_posteriors(fem_em *h, double *post);
 /* EMAlgorithm::RetrieveClasses (EM2/EMAlgorithm.cpp:107-122) */
 int fem_em_retrieve_classes(fem_em *h, int32_t *classes);
+/* EMAlgorithm::ComputePosterriorCorrelation (EM2/EMAlgorithm.cpp:213-219):
+ * corr = R^T R (k x k, row-major) over the posteriors of the last E-step,
+ * computed on the device */
+int fem_em_posterior_correlation(fem_em *h, double *corr);
 /* NormalDensity::GetInvertedCholCov / GetLogDeterminant
  * (EM2/NormalDensity.h:42,45): U_j = (L_j^-1)^T upper, k*d*d, and logdet[k] */
 int fem_em_get_factors(fem_em *h, double *U, double *logdet);

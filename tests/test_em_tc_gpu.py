@@ -119,3 +119,49 @@ def test_tc_sweeps_small_components(gpu_lib, oracle):
     covariance operands averages over 16x fewer points, tolerance 3e-5."""
     err, G, ref = run_sweeps(oracle, 1 << 17, 32, 8)
     assert err.max() <= 3e-5
+
+
+# ------------------------------------------------- d < 64 and K not a multiple of 4
+@pytest.mark.parametrize("d,k", [(8, 10), (4, 3), (16, 7), (32, 32), (63, 5)])
+def test_tc_padded_dims_and_components(gpu_lib, oracle, d, k):
+    """d < 64 runs zero-padded to 64 dimensions, K is padded to a multiple of 4
+    with zero-weight components; sweeps against the FP64 oracle."""
+    n = 40000
+    X, _ = synth.kmeans_blobs(seed=5, n=n, d=d, k=k, spread=5.0, sigma=1.0)
+    init = synth.dsquared_init(X, k, seed=2)
+    ref = oracle.em_train(X, *init, 10, eps=0.0)
+    with CudaMatrixEM(d, n, k, precision="mixed") as em:
+        em.SetParameters(10, 0.0, 1e5)
+        G = GaussianMixture(*init)
+        em.Train(X, G)
+        ll = em.logl_trace
+    err = np.abs(ll - ref["logl"]) / n
+    print("padded d=%d k=%d |dlogL/N| per sweep: %s" % (d, k, " ".join("%.2e" % e for e in err)))
+    assert err.max() <= 1e-5
+    np.testing.assert_allclose(G.weights, ref["pi"], rtol=1e-3, atol=1e-6)
+    assert G.means.shape == (k, d) and G.covs.shape == (k, d, d)
+
+
+def test_tc_batched_fits_subset(gpu_lib, oracle):
+    """The first fits of the 512-fit batched workload (N log-uniform in
+    [2e3, 2e5], d in {4, 8, 16, 32}, K in [2, 32], blob data): 30 mixed
+    sweeps each, per-fit |dlogL/N| against the FP64 oracle."""
+    worst = 0.0
+    for f in synth.em_batched()[:6]:
+        X, _ = synth.kmeans_blobs(seed=f["seed"], n=f["n"], d=f["d"], k=f["k"])
+        init = synth.dsquared_init(X, f["k"], seed=f["seed"] % 1000)
+        ref = oracle.em_train(X, *init, 30, eps=0.0)
+        with CudaMatrixEM(f["d"], f["n"], f["k"], precision="mixed") as em:
+            em.SetParameters(30, 0.0, 1e5)
+            G = GaussianMixture(*init)
+            try:
+                em.Train(X, G)
+            except Exception as e:   # the oracle must then fail the same way
+                assert ref["status"] != 0, str(e)
+                continue
+            ll = em.logl_trace
+        m = len(ll)
+        err = np.abs(ll - ref["logl"][:m]) / f["n"]
+        worst = max(worst, err.max())
+        print("fit n=%d d=%d k=%d sweeps=%d max |dlogL/N| %.2e" % (f["n"], f["d"], f["k"], m, err.max()))
+    assert worst <= 1e-5

@@ -105,7 +105,7 @@ def test_em2gpu_fp64_matches_oracle(em2gpu, oracle, tmp_path):
 
 
 @pytest.mark.gpu
-def test_em2gpu_kmeans_init_and_unsupported_precision(em2gpu, tmp_path):
+def test_em2gpu_kmeans_init_mixed_and_unsupported_width(em2gpu, tmp_path):
     X, _ = synth.kmeans_blobs(seed=3, n=20000, d=8, k=6)
     fb = str(tmp_path / "b.bin")
     formats.write_bin(fb, X)
@@ -114,7 +114,12 @@ def test_em2gpu_kmeans_init_and_unsupported_precision(em2gpu, tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     final = float(out.stdout.split("Final loglikelihood:")[1].split()[0])
     assert np.isfinite(final)
-    # the mixed-precision E/M kernels are built for d = 64: d = 8 is refused with a message
-    bad = subprocess.run([em2gpu, fb, "-c", "6", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
+    # mixed precision runs d <= 64 (zero-padded); d = 80 is refused with a message
+    ok = subprocess.run([em2gpu, fb, "-c", "6", "-p", "mixed", "-m", "3", "-I", "kmeans"], capture_output=True,
+                        text=True, timeout=300)
+    assert ok.returncode == 0, ok.stdout + ok.stderr
+    fw = str(tmp_path / "wide.bin")
+    formats.write_bin(fw, np.random.default_rng(1).standard_normal((5000, 80)).astype(np.float32))
+    bad = subprocess.run([em2gpu, fw, "-c", "4", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
                          timeout=300)
     assert bad.returncode == 1 and "mixed precision" in bad.stderr
