@@ -42,8 +42,9 @@ constexpr int kKmAccPitch = kKmD + 1;    // padded rows of the fixed-point sums
 constexpr int kKmThreads = 14 * 32;
 constexpr uint32_t kKmXBytes = kKmTile * kKmD * 4;       // 16 KB FP32 tile
 // bound constants (see k_km_tc_prep)
-constexpr float kKmRel = 1.220703125e-4f;                 // 2^-13
+constexpr float kKmRel = 1.8310546875e-4f;                // 2^-13 + 2^-14
 constexpr float kKmAbs = 3.814697265625e-6f;              // 2^-18
+constexpr float kKmPad = 3.0e38f;                         // v of padding centroids
 
 struct __align__(1024) KmSmem {
   __half b1[kKmMaxK * 64];                 // [ch | ch]  (SW128)
@@ -92,10 +93,12 @@ __global__ void k_km_tc_prep(const double *__restrict__ cent, const double *__re
     double s = 0.0;
     for (int t = 0; t < kKmD; t++) s += red[t];
     const float n2 = (float)s, nrm = (float)sqrt(s);
-    // |v_j - (||c'||^2 - 2 x'.c')| <= ||x'|| bc_j + ac_j + ax(||x'||)  (v in FP32)
-    cconst[j] = j < K ? n2 : INFINITY;
+    // |v_j - (||c'||^2 - 2 x'.c')| <= ||x'|| bc_j + ac_j + ax(||x'||)  (v in FP32);
+    // 2^-14 ||x'|| ||c'|| + 2^-15 ||c'||^2 of it cover the centroid index kept
+    // in the low 8 bits of the scanned values (at most 2^-15 |v|)
+    cconst[j] = j < K ? n2 : kKmPad;
     cconst[Kp + j] = j < K ? kKmRel * nrm : 0.f;
-    const float a = j < K ? kKmAbs * nrm + 9.5367431640625e-7f * n2 + 1e-30f : 0.f;   // 2^-20
+    const float a = j < K ? kKmAbs * nrm + 3.147125244140625e-5f * n2 + 1e-30f : 0.f;   // 2^-15 + 2^-20
     cconst[2 * Kp + j] = a;
     // maxima over the centroids (non-negative floats order like their bits)
     atomicMax(reinterpret_cast<int *>(cconst + 3 * Kp), __float_as_int(cconst[Kp + j]));
@@ -170,7 +173,7 @@ k_km_assign_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__
   for (int e = threadIdx.x; e < kKmMaxK * kKmAccPitch; e += blockDim.x) S.acc[e] = 0;
   for (int j = threadIdx.x; j < kKmMaxK; j += blockDim.x) {
     S.cnt[j] = 0;
-    S.cn2[j] = j < Kp ? cconst[j] : INFINITY;
+    S.cn2[j] = j < Kp ? cconst[j] : kKmPad;
     S.bc[j] = j < Kp ? cconst[Kp + j] : 0.f;
     S.ac[j] = j < Kp ? cconst[2 * Kp + j] : 0.f;
   }
@@ -285,25 +288,36 @@ k_km_assign_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__
       const int s = (int)(i % kKmXStages);
       if (!(ok = mbar_wait_warp(&S.acc_full[g], (i >> 1) & 1, err))) break;
       tc_fence_after();
-      // the two smallest v with their indices, and the third smallest value
-      float v1 = INFINITY, v2 = INFINITY, v3 = INFINITY;
-      int j1 = 0, j2 = 0;
+      // the three smallest v; the centroid index rides in the low 8 bits of
+      // each value (v changes by at most 2^-15 |v|, which the bound covers),
+      // so the scan is a min/max network without index bookkeeping
+      float m1 = kKmPad, m2 = kKmPad, m3 = kKmPad;
+      auto scan = [&](float v, int j) {
+        const float e = __int_as_float((__float_as_int(v) & ~0xFF) | j);
+        const float hi = fmaxf(m1, e);
+        m1 = fminf(m1, e);
+        const float hi2 = fmaxf(m2, hi);
+        m2 = fminf(m2, hi);
+        m3 = fminf(m3, hi2);
+      };
+      int c0 = 0;
 #pragma unroll 1
-      for (int c0 = 0; c0 < Kp; c0 += 32) {
+      for (; c0 + 32 <= Kp; c0 += 32) {
         uint32_t dv[32];
         tmem_ld32(tbase + lane_addr + g * kKmMaxK + c0, dv);
         tmem_wait_ld();
 #pragma unroll
-        for (int t = 0; t < 32; t++) {
-          const float v = fmaf(-2.f, __uint_as_float(dv[t]), S.cn2[c0 + t]);
-          const bool lt1 = v < v1, lt2 = v < v2;
-          v3 = lt2 ? v2 : fminf(v3, v);
-          v2 = lt1 ? v1 : (lt2 ? v : v2);
-          j2 = lt1 ? j1 : (lt2 ? c0 + t : j2);
-          v1 = lt1 ? v : v1;
-          j1 = lt1 ? c0 + t : j1;
-        }
+        for (int t = 0; t < 32; t++) scan(fmaf(-2.f, __uint_as_float(dv[t]), S.cn2[c0 + t]), c0 + t);
       }
+      if (c0 < Kp) {                             // Kp is a multiple of 16
+        uint32_t dv[16];
+        tmem_ld16(tbase + lane_addr + g * kKmMaxK + c0, dv);
+        tmem_wait_ld();
+#pragma unroll
+        for (int t = 0; t < 16; t++) scan(fmaf(-2.f, __uint_as_float(dv[t]), S.cn2[c0 + t]), c0 + t);
+      }
+      const int j1 = __float_as_int(m1) & 0xFF, j2 = __float_as_int(m2) & 0xFF;
+      const float v1 = m1, v2 = m2, v3 = m3;
       const int64_t row = (blockIdx.x + i * gridDim.x) * kKmTile + r;
       const float *xs = S.x[s] + r * kKmD;
       const float xn = S.xn[s][r];
