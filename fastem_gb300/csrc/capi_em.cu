@@ -95,17 +95,7 @@ int enqueue_mstep(fem_em *h) {
   return FEM_OK;
 }
 
-int max_cond(fem_em *h, double *cond) {
-  const size_t dd = (size_t)h->d * h->d;
-  std::vector<double> S(dd * h->k);
-  FEM_CUDA(cudaMemcpyAsync(S.data(), h->sigma, S.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                           h->stream));
-  FEM_CUDA(cudaStreamSynchronize(h->stream));
-  double mx = 0.0;
-  for (int j = 0; j < h->k; j++) mx = std::max(mx, host_cond_number(h->d, S.data() + dd * j));
-  *cond = mx;
-  return FEM_OK;
-}
+int max_cond(fem_em *h, double *cond) { return em_max_cond(h, cond); }
 
 void free_all(fem_em *h) {
   if (h->tc) em_tc_destroy(h);

@@ -79,47 +79,6 @@ int encode_tmap_2d(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, const
   return FEM_OK;
 }
 
-// NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71) on the
-// host: cyclic Jacobi eigenvalues of sym(lower(sigma)), |l_max / l_min|.
-double host_cond_number(int d, const double *sigma) {
-  std::vector<double> A((size_t)d * d);
-  for (int r = 0; r < d; r++)
-    for (int c = 0; c < d; c++) A[(size_t)r * d + c] = (c <= r) ? sigma[(size_t)r * d + c] : sigma[(size_t)c * d + r];
-  for (int sweep = 0; sweep < 100; sweep++) {
-    double off = 0.0, diag = 0.0;
-    for (int p = 0; p < d; p++) {
-      diag += A[(size_t)p * d + p] * A[(size_t)p * d + p];
-      for (int q = p + 1; q < d; q++) off += A[(size_t)p * d + q] * A[(size_t)p * d + q];
-    }
-    if (off <= 1e-30 * diag) break;
-    for (int p = 0; p < d; p++)
-      for (int q = p + 1; q < d; q++) {
-        const double apq = A[(size_t)p * d + q];
-        if (apq == 0.0) continue;
-        const double app = A[(size_t)p * d + p], aqq = A[(size_t)q * d + q];
-        const double th = (aqq - app) / (2.0 * apq);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int r = 0; r < d; r++) {
-          const double arp = A[(size_t)r * d + p], arq = A[(size_t)r * d + q];
-          A[(size_t)r * d + p] = c * arp - s * arq;
-          A[(size_t)r * d + q] = s * arp + c * arq;
-        }
-        for (int r = 0; r < d; r++) {
-          const double apr = A[(size_t)p * d + r], aqr = A[(size_t)q * d + r];
-          A[(size_t)p * d + r] = c * apr - s * aqr;
-          A[(size_t)q * d + r] = s * apr + c * aqr;
-        }
-      }
-  }
-  double mn = A[0], mx = A[0];
-  for (int p = 1; p < d; p++) {
-    mn = std::fmin(mn, A[(size_t)p * d + p]);
-    mx = std::fmax(mx, A[(size_t)p * d + p]);
-  }
-  return std::fabs(mx / mn);
-}
-
 }  // namespace fem
 
 extern "C" int fem_api_version(void) { return FEM_API_VERSION; }

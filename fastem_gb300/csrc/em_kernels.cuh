@@ -30,6 +30,7 @@ int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);
 int em_tc_classes(fem_em *h, int32_t *dcls);
 
 // host_linalg.cpp
-double host_cond_number(int d, const double *sigma);
+// largest condition number of the K covariances (FP64 Jacobi on the device)
+int em_max_cond(fem_em *h, double *cond);
 
 }  // namespace fem

@@ -12,6 +12,7 @@
 // multiplies by CholInvC = W_j^T from the right, EM2/MatrixEM.cpp:76).
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 
 #include "fem_internal.cuh"
 #include "em_kernels.cuh"
@@ -601,6 +602,123 @@ static int mstep_plain_t(fem_em *h) {
 
 int em_plain_mstep(fem_em *h) {
   return h->cfg.precision == FEM_PREC_FP64 ? mstep_plain_t<double>(h) : mstep_plain_t<float>(h);
+}
+
+// NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71): the
+// eigenvalues of each Sigma_j by cyclic Jacobi in FP64, one CTA per
+// component, on a copy in `work`.  Each sweep runs the n - 1 rounds of a
+// round-robin schedule; a round rotates n / 2 disjoint (p, q) pairs at once
+// (columns, then rows).  Sweeps stop when the off-diagonal mass is below
+// 1e-30 of the diagonal's, or after 100.  cond_j = |max eig / min eig|; the
+// largest over j is folded into *out (non-negative doubles order like their bits).
+__global__ void __launch_bounds__(256)
+k_cond_jacobi(const double *__restrict__ sigma, int d, double *__restrict__ work, unsigned long long *out) {
+  const int j = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  double *A = work + (size_t)j * d * d;
+  const double *S = sigma + (size_t)j * d * d;
+  const int n = d + (d & 1);          // players of the round robin (a dummy when d is odd)
+  const int np = n / 2;
+  __shared__ double sc[128], ss[128];
+  __shared__ int sp[128], sq[128];
+  __shared__ double red_off[256], red_diag[256];
+  __shared__ int done;
+  for (int e = tid; e < d * d; e += nt) {
+    const int r = e / d, c = e - r * d;
+    A[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
+  }
+  __syncthreads();
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, dg = 0.0;
+    for (int e = tid; e < d * d; e += nt) {
+      const int r = e / d, c = e - r * d;
+      const double v = A[e];
+      if (c > r) off += v * v;
+      else if (c == r) dg += v * v;
+    }
+    red_off[tid] = off;
+    red_diag[tid] = dg;
+    __syncthreads();
+    if (tid == 0) {
+      double o = 0.0, g = 0.0;
+      for (int t = 0; t < nt; t++) o += red_off[t], g += red_diag[t];
+      done = !(o > 1e-30 * g);
+    }
+    __syncthreads();
+    if (done) break;
+    for (int round = 0; round < n - 1; round++) {
+      for (int i = tid; i < np; i += nt) {
+        // position m holds player 0 (m = 0) or 1 + (m - 1 + round) mod (n - 1)
+        const int m1 = i, m2 = n - 1 - i;
+        const int p0 = m1 == 0 ? 0 : 1 + (m1 - 1 + round) % (n - 1);
+        const int q0 = 1 + (m2 - 1 + round) % (n - 1);
+        const int p = min(p0, q0), q = max(p0, q0);
+        double c = 1.0, s = 0.0;
+        if (q < d) {
+          const double apq = A[(size_t)p * d + q];
+          if (apq != 0.0) {
+            const double app = A[(size_t)p * d + p], aqq = A[(size_t)q * d + q];
+            const double th = (aqq - app) / (2.0 * apq);
+            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+          }
+        }
+        sc[i] = c, ss[i] = s, sp[i] = p, sq[i] = q;
+      }
+      __syncthreads();
+      for (int e = tid; e < d * np; e += nt) {     // columns p, q of every row
+        const int i = e / d, r = e - i * d;
+        const int p = sp[i], q = sq[i];
+        if (q < d && ss[i] != 0.0) {
+          const double arp = A[(size_t)r * d + p], arq = A[(size_t)r * d + q];
+          A[(size_t)r * d + p] = sc[i] * arp - ss[i] * arq;
+          A[(size_t)r * d + q] = ss[i] * arp + sc[i] * arq;
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < d * np; e += nt) {     // rows p, q of every column
+        const int i = e / d, r = e - i * d;
+        const int p = sp[i], q = sq[i];
+        if (q < d && ss[i] != 0.0) {
+          const double apr = A[(size_t)p * d + r], aqr = A[(size_t)q * d + r];
+          A[(size_t)p * d + r] = sc[i] * apr - ss[i] * aqr;
+          A[(size_t)q * d + r] = ss[i] * apr + sc[i] * aqr;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (tid == 0) {
+    double mn = A[0], mx = A[0];
+    for (int p = 1; p < d; p++) {
+      mn = fmin(mn, A[(size_t)p * d + p]);
+      mx = fmax(mx, A[(size_t)p * d + p]);
+    }
+    atomicMax(out, (unsigned long long)__double_as_longlong(fabs(mx / mn)));
+  }
+}
+
+int em_max_cond(fem_em *h, double *cond) {
+  if (h->d > 256) {
+    set_error("condition check supports d <= 256 (got %d)", h->d);
+    return FEM_ERR_UNSUPPORTED;
+  }
+  unsigned long long *dout = nullptr;
+  FEM_TRY(dalloc(&dout, 1));
+  FEM_CUDA(cudaMemsetAsync(dout, 0, sizeof(unsigned long long), h->stream));
+  k_cond_jacobi<<<h->k, 256, 0, h->stream>>>(h->sigma, h->d, h->work, dout);
+  cudaError_t e = cudaGetLastError();
+  unsigned long long bits = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, dout, sizeof(bits), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  dfree(dout);
+  if (e != cudaSuccess) {
+    set_error("condition-number kernel failed: %s", cudaGetErrorString(e));
+    return FEM_ERR_CUDA;
+  }
+  std::memcpy(cond, &bits, sizeof(double));
+  h->launches += 1;
+  return FEM_OK;
 }
 
 int em_factor(fem_em *h, bool regularize) {

@@ -164,3 +164,23 @@ def test_em_condition_abort(gpu_lib):
         with pytest.raises(C.ConditionAbort):
             em.TrainNoCopy(GaussianMixture(np.array([0.5, 0.5]), X[:2].astype(np.float64), ill), svd=True)
         assert em.FindLargestConditionNumber() == pytest.approx(1e6, rel=1e-9)
+
+
+@pytest.mark.parametrize("d,k,precision", [(8, 5, "fp64"), (63, 3, "fp32"), (64, 4, "mixed"), (200, 2, "fp64")])
+def test_condition_number_on_device(gpu_lib, d, k, precision):
+    """FindLargestConditionNumber: FP64 Jacobi eigenvalues on the device
+    against numpy (odd d uses a dummy in the round-robin schedule)."""
+    rng = np.random.default_rng(d)
+    covs = np.empty((k, d, d))
+    for j in range(k):
+        Q = synth.haar_orthogonal(rng, d)
+        lam = np.logspace(-2 - j, 2, d)
+        covs[j] = 0.5 * ((Q * lam) @ Q.T + ((Q * lam) @ Q.T).T)
+    G = GaussianMixture(np.full(k, 1.0 / k), rng.standard_normal((k, d)), covs)
+    with CudaMatrixEM(d, 1000, k, precision=precision) as em:
+        em.SetMixture(G)
+        c = em.FindLargestConditionNumber()
+    ev = np.linalg.eigvalsh(covs)
+    ref = np.max(np.abs(ev.max(axis=1) / ev.min(axis=1)))
+    # the smallest eigenvalue carries an FP64 error of ~||Sigma|| eps in any solver
+    assert abs(c / ref - 1) <= max(1e-9, 100 * ref * np.finfo(float).eps), (c, ref)
