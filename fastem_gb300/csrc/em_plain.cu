@@ -604,6 +604,8 @@ int em_plain_mstep(fem_em *h) {
   return h->cfg.precision == FEM_PREC_FP64 ? mstep_plain_t<double>(h) : mstep_plain_t<float>(h);
 }
 
+constexpr size_t kJacobiSmem = 96 * 1024;
+
 // NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71): the
 // eigenvalues of each Sigma_j by cyclic Jacobi in FP64, one CTA per
 // component, on a copy in `work`.  Each sweep runs the n - 1 rounds of a
@@ -613,8 +615,10 @@ int em_plain_mstep(fem_em *h) {
 // largest over j is folded into *out (non-negative doubles order like their bits).
 __global__ void __launch_bounds__(256)
 k_cond_jacobi(const double *__restrict__ sigma, int d, double *__restrict__ work, unsigned long long *out) {
+  extern __shared__ double smem_jac[];
   const int j = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  double *A = work + (size_t)j * d * d;
+  // the matrix lives in shared memory when it fits (d <= 110), else in `work`
+  double *A = (size_t)d * d * sizeof(double) <= kJacobiSmem ? smem_jac : work + (size_t)j * d * d;
   const double *S = sigma + (size_t)j * d * d;
   const int n = d + (d & 1);          // players of the round robin (a dummy when d is odd)
   const int np = n / 2;
@@ -706,7 +710,9 @@ int em_max_cond(fem_em *h, double *cond) {
   unsigned long long *dout = nullptr;
   FEM_TRY(dalloc(&dout, 1));
   FEM_CUDA(cudaMemsetAsync(dout, 0, sizeof(unsigned long long), h->stream));
-  k_cond_jacobi<<<h->k, 256, 0, h->stream>>>(h->sigma, h->d, h->work, dout);
+  const size_t sm = (size_t)h->d * h->d * sizeof(double) <= kJacobiSmem ? (size_t)h->d * h->d * sizeof(double) : 0;
+  if (sm > 48 * 1024) FEM_CUDA(cudaFuncSetAttribute(k_cond_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_cond_jacobi<<<h->k, 256, sm, h->stream>>>(h->sigma, h->d, h->work, dout);
   cudaError_t e = cudaGetLastError();
   unsigned long long bits = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, dout, sizeof(bits), cudaMemcpyDeviceToHost, h->stream);
