@@ -107,6 +107,13 @@ void orc_km_oror(int d, int64_t n, int k, const float *X, double oversample,
 /* ForgyInitializer::Init (Clust/KMeansInitializer.cpp:33-49). */
 void orc_km_forgy(int d, int64_t n, int k, const float *X, double *centroids);
 
+/* One sweep (factorise, E-step with logL, M-step) organised like
+ * SimpleMatrixEM with level-3 BLAS: for CPU timing (fem_oracle_blas.cpp).  The
+ * CBLAS dtrmm / dgemm / dsyrk entry points are supplied by the caller.
+ * pi, mu, sigma are updated in place; *logl is the pre-M-step logL. */
+int orc_em_sweep_blas(int d, int64_t n, int k, const float *X, double *pi, double *mu, double *sigma,
+                      double *logl, int nthreads, void *dtrmm, void *dgemm, void *dsyrk);
+
 #ifdef __cplusplus
 }
 #endif

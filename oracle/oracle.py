@@ -40,8 +40,7 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(_HERE, "liboracle.so")
-        if not os.path.exists(path):
-            build()
+        build()                       # make: a no-op when the library is up to date
         L = ctypes.CDLL(path)
         P = ctypes.c_void_p
         i32, i64, f64 = ctypes.c_int, ctypes.c_int64, ctypes.c_double
@@ -62,6 +61,7 @@ def lib():
         L.orc_km_plusplus.argtypes = [i32, i64, i32, P, P, P]
         L.orc_km_oror.argtypes = [i32, i64, i32, P, f64, P, i32]
         L.orc_km_forgy.argtypes = [i32, i64, i32, P, P]
+        L.orc_em_sweep_blas.argtypes = [i32, i64, i32, P, P, P, P, P, i32, P, P, P]
         _LIB = L
     return _LIB
 
@@ -203,3 +203,51 @@ def kmeans_forgy(X, k, seed=None):
     out = np.zeros((k, d))
     lib().orc_km_forgy(d, n, k, _p(X), _p(out))
     return out
+
+
+_BLAS = None
+
+
+def openblas():
+    """scipy's bundled OpenBLAS (CBLAS entry points named scipy_cblas_*), set
+    to one thread (the oracle's OpenMP threads each call it); None if absent."""
+    global _BLAS
+    if _BLAS is None:
+        import glob
+        try:
+            import scipy
+        except ImportError:
+            return None
+        libs = sorted(glob.glob(os.path.join(os.path.dirname(scipy.__file__), "..", "scipy.libs",
+                                             "libscipy_openblas*.so*")))
+        for path in libs:
+            try:
+                B = ctypes.CDLL(path)
+                fns = [ctypes.cast(getattr(B, "scipy_cblas_" + f), ctypes.c_void_p).value
+                       for f in ("dtrmm", "dgemm", "dsyrk")]
+            except (OSError, AttributeError):
+                continue
+            if hasattr(B, "scipy_openblas_set_num_threads"):
+                B.scipy_openblas_set_num_threads(1)
+            _BLAS = (B, fns)
+            break
+    return _BLAS
+
+
+def em_sweep_blas(X, pi, mu, sigma, nthreads=0):
+    """One FP64 sweep organised like SimpleMatrixEM with OpenBLAS level-3
+    calls (orc_em_sweep_blas).  Returns (logL, pi, mu, sigma)."""
+    blas = openblas()
+    if blas is None:
+        raise RuntimeError("scipy's bundled OpenBLAS was not found")
+    X = _f32(X)
+    n, d = X.shape
+    pi = np.array(pi, dtype=np.float64, copy=True)
+    mu = np.array(mu, dtype=np.float64, copy=True, order="C")
+    sigma = np.array(sigma, dtype=np.float64, copy=True, order="C")
+    ll = ctypes.c_double(np.nan)
+    st = lib().orc_em_sweep_blas(d, n, len(pi), _p(X), _p(pi), _p(mu), _p(sigma), ctypes.byref(ll),
+                                 int(nthreads), *[ctypes.c_void_p(f) for f in blas[1]])
+    if st != ORC_OK:
+        raise RuntimeError("orc_em_sweep_blas failed with status %d" % st)
+    return ll.value, pi, mu, sigma

@@ -160,3 +160,18 @@ def test_seeders_deterministic(oracle):
     # every seed is a data row
     rows = {tuple(r) for r in X.astype(np.float64)}
     assert all(tuple(r) in rows for r in p)
+
+
+def test_blas_sweep_matches_oracle(oracle):
+    """The BLAS-organised sweep used for CPU timing gives the oracle's sweep."""
+    if oracle.openblas() is None:
+        pytest.skip("scipy's bundled OpenBLAS not found")
+    from fastem_gb300 import synth
+    X, _ = synth.em_large(seed=3, n=4000, d=16, k=6)
+    pi, mu, sg = synth.dsquared_init(X, 6, seed=5)
+    ll, pi2, mu2, sg2 = oracle.em_sweep_blas(X, pi, mu, sg)
+    ref = oracle.em_train(X, pi, mu, sg, 1, eps=0.0)
+    assert abs(ll - ref["logl"][0]) <= 1e-11 * abs(ref["logl"][0])
+    np.testing.assert_allclose(pi2, ref["pi"], rtol=1e-11)
+    np.testing.assert_allclose(mu2, ref["mu"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(sg2, ref["sigma"], rtol=1e-9, atol=1e-12)
