@@ -210,6 +210,14 @@ int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **ou
   if (c.precision == FEM_PREC_MIXED) {
     st = em_tc_create(h);
     if (st) return fail(st);
+    if (em_tc_small_components(n, k)) {
+      // partials of the FP32 CUDA-core covariance used for small components
+      int TB, nb, nblk;
+      cov_geometry(d, &TB, &nb, &nblk);
+      const int gx = (k * nblk + 255) / 256;
+      h->cchunks = (int)std::max<int64_t>(1, std::min<int64_t>((3 * sm_count() + gx - 1) / gx, (n + 31) / 32));
+      if ((st = dalloc(&h->cpart, (size_t)h->cchunks * k * nblk * TB * TB))) return fail(st);
+    }
   } else {
     h->n_logl_part = em_plain_logl_blocks(n, d);
     if ((st = dalloc(&h->logl_part, h->n_logl_part))) return fail(st);

@@ -22,6 +22,11 @@ int em_tc_upload(fem_em *h);    // X -> bf16 hi/lo split
 int em_tc_prepare(fem_em *h);   // factors -> permuted bf16 hi/lo operands + offsets
 int em_tc_estep(fem_em *h);
 int em_tc_mstep(fem_em *h);
+// the mixed path's covariance on CUDA cores in FP32 (for small components):
+// posteriors as FP16 hi + lo, means as float with row stride mu_ld
+int em_cov_hilo(fem_em *h, const __half *Rh, const __half *Rl, int64_t pitch, const float *muf, int mu_ld);
+// true when the mixed path computes covariances with em_cov_hilo
+bool em_tc_small_components(int64_t n, int k);
 // device posteriors of the mixed path: FP16 hi / lo, component-major, row pitch
 void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch);
 // records event `slot` on the handle's stream when timing is enabled

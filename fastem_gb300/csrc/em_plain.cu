@@ -271,11 +271,27 @@ __global__ void k_final_means(const double *__restrict__ part, int G, int K, int
 // of one component; a CTA owns 256 consecutive (component, block) units.
 constexpr int kCovTP = 32;
 
-template <typename T, int TB>
+// posterior (component j, point i): typed component-major array, or the
+// mixed path's FP16 hi + lo pair
+template <typename T>
+struct PostTyped {
+  const T *R;
+  int64_t pitch;
+  __device__ T operator()(int j, int64_t i) const { return R[(size_t)j * pitch + i]; }
+};
+struct PostHiLo {
+  const __half *Rh, *Rl;
+  int64_t pitch;
+  __device__ float operator()(int j, int64_t i) const {
+    const size_t o = (size_t)j * pitch + i;
+    return __half2float(Rh[o]) + __half2float(Rl[o]);
+  }
+};
+
+template <typename T, int TB, class Src>
 __global__ void __launch_bounds__(256)
-k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__restrict__ R,
-            const T *__restrict__ mu, double *__restrict__ part, int nb, int nblk,
-            int64_t rows_per_chunk) {
+k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T *__restrict__ mu, int mu_ld,
+            double *__restrict__ part, int nb, int nblk, int64_t rows_per_chunk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *sZ = (T *)smem_raw;  // CJ x TP x d
   const int tid = threadIdx.x;
@@ -315,8 +331,8 @@ k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__res
       T z = T(0);
       if (p < tp) {
         const int64_t row = t0 + p;
-        const T r = R[(size_t)(j_lo + jj) * n + row];
-        z = sqrt(r) * ((T)X[row * d + a] - mu[(size_t)(j_lo + jj) * d + a]);
+        const T r = (T)R(j_lo + jj, row);
+        z = sqrt(r) * ((T)X[row * d + a] - mu[(size_t)(j_lo + jj) * mu_ld + a]);
       }
       sZ[e] = z;
     }
@@ -513,9 +529,11 @@ int64_t em_plain_logl_blocks(int64_t n, int d) {
   }
 }
 
+// tiles of TB x TB covariance entries; TB divides d, so no tile reaches past
+// the last dimension
 void cov_geometry(int d, int *TB, int *nb, int *nblk) {
-  *TB = d >= 8 ? 8 : d;
-  *nb = (d + *TB - 1) / *TB;
+  *TB = d % 8 == 0 ? 8 : (d % 4 == 0 ? 4 : (d % 2 == 0 ? 2 : 1));
+  *nb = d / *TB;
   *nblk = (*nb) * (*nb + 1) / 2;
 }
 
@@ -539,18 +557,46 @@ static int launch_means(fem_em *h, int upt, int64_t rpb, size_t sm) {
   return FEM_ERR_UNSUPPORTED;
 }
 
-template <typename T, int TB>
-static int launch_cov(fem_em *h, int nb, int nblk, int64_t rpc) {
+template <typename T, int TB, class Src>
+static int launch_cov(fem_em *h, int nb, int nblk, int64_t rpc, Src src, const T *mu, int mu_ld) {
   const int units = h->k * nblk;
   const int gx = (units + 255) / 256;
   const int cjmax = 256 / nblk + 2;
   size_t sm = (size_t)min(cjmax, h->k) * kCovTP * h->d * sizeof(T);
   if (sm > 48 * 1024)
-    FEM_CUDA(cudaFuncSetAttribute(k_cov_plain<T, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    FEM_CUDA(cudaFuncSetAttribute(k_cov_plain<T, TB, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)sm));
   dim3 grid(gx, h->cchunks);
-  k_cov_plain<T, TB><<<grid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, (const T *)h->R,
-                                                   (const T *)h->muT, h->cpart, nb, nblk, rpc);
+  k_cov_plain<T, TB, Src><<<grid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, src, mu, mu_ld, h->cpart, nb,
+                                                        nblk, rpc);
+  return FEM_OK;
+}
+
+// the covariance pass for any posterior source: partials + FP64 finalisation
+template <typename T, class Src>
+static int cov_pass(fem_em *h, Src src, const T *mu, int mu_ld) {
+  const int d = h->d, K = h->k;
+  int TB, nb, nblk, st;
+  cov_geometry(d, &TB, &nb, &nblk);
+  const int64_t rpc = (h->n + h->cchunks - 1) / h->cchunks;
+  if (TB == 8)
+    st = launch_cov<T, 8>(h, nb, nblk, rpc, src, mu, mu_ld);
+  else if (TB == 4)
+    st = launch_cov<T, 4>(h, nb, nblk, rpc, src, mu, mu_ld);
+  else if (TB == 2)
+    st = launch_cov<T, 2>(h, nb, nblk, rpc, src, mu, mu_ld);
+  else
+    st = launch_cov<T, 1>(h, nb, nblk, rpc, src, mu, mu_ld);
+  FEM_TRY(st);
+  FEM_CUDA(cudaGetLastError());
+  k_final_cov<<<K, 256, 0, h->stream>>>(h->cpart, h->cchunks, K, d, nb, nblk, TB, h->psum, h->sigma);
+  FEM_CUDA(cudaGetLastError());
+  return FEM_OK;
+}
+
+int em_cov_hilo(fem_em *h, const __half *Rh, const __half *Rl, int64_t pitch, const float *muf, int mu_ld) {
+  FEM_TRY((cov_pass<float, PostHiLo>(h, PostHiLo{Rh, Rl, pitch}, muf, mu_ld)));
+  h->launches += 2;
   return FEM_OK;
 }
 
@@ -580,22 +626,7 @@ static int mstep_plain_t(fem_em *h) {
   k_final_means<T><<<K, 128, 0, h->stream>>>(h->mpart, h->mgrid, K, d, n, h->mu, h->pi, h->psum,
                                              (T *)h->muT);
   FEM_CUDA(cudaGetLastError());
-  int TB, nb, nblk;
-  cov_geometry(d, &TB, &nb, &nblk);
-  const int64_t rpc = (n + h->cchunks - 1) / h->cchunks;
-  if (TB == 8)
-    st = launch_cov<T, 8>(h, nb, nblk, rpc);
-  else if (TB == 4)
-    st = launch_cov<T, 4>(h, nb, nblk, rpc);
-  else if (TB == 2)
-    st = launch_cov<T, 2>(h, nb, nblk, rpc);
-  else
-    st = launch_cov<T, 1>(h, nb, nblk, rpc);
-  FEM_TRY(st);
-  FEM_CUDA(cudaGetLastError());
-  k_final_cov<<<K, 256, 0, h->stream>>>(h->cpart, h->cchunks, K, d, nb, nblk, TB, h->psum,
-                                        h->sigma);
-  FEM_CUDA(cudaGetLastError());
+  FEM_TRY((cov_pass<T, PostTyped<T>>(h, PostTyped<T>{(const T *)h->R, n}, (const T *)h->muT, d)));
   h->launches += 4;
   return FEM_OK;
 }

@@ -910,6 +910,12 @@ static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t ro
 // d <= 64 (zero-padded to 64) and K <= 128 (padded to a multiple of 4)
 bool em_tc_supported(int d, int k) { return d >= 1 && d <= kD && k >= 1 && k <= kMaxK; }
 
+// The tensor-core covariance rounds z to FP16 once; that error averages out
+// over the points of a component (relative ~2^-12 / sqrt(N_j)).  With fewer
+// than 16384 points per component on average it would not, so such fits take
+// the FP32 CUDA-core covariance (its cost is small at that size).
+bool em_tc_small_components(int64_t n, int k) { return n < (int64_t)16384 * k; }
+
 int em_tc_create(fem_em *h) {
   TcEmPlan *p = new TcEmPlan();
   h->tc = p;
@@ -1049,6 +1055,14 @@ int em_tc_mstep(fem_em *h) {
   FEM_CUDA(cudaGetLastError());
   k_final_means_tc<<<K, 64, 0, h->stream>>>(p->mpart, p->mgrid, K, h->d, h->n, h->mu, h->pi, h->psum, p->muf);
   FEM_CUDA(cudaGetLastError());
+  if (em_tc_small_components(h->n, h->k)) {
+    timing_begin(h, 8);
+    FEM_TRY(em_cov_hilo(h, p->Rh, p->Rl, p->np, p->muf, kD));
+    timing_begin(h, 9);
+    k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
+    h->launches += 3;
+    return FEM_OK;
+  }
   const int64_t nblocks = (h->n + kBlk - 1) / kBlk;
   const int64_t bpc = (nblocks + p->cgy - 1) / p->cgy;
   timing_begin(h, 8);
