@@ -184,3 +184,24 @@ def test_condition_number_on_device(gpu_lib, d, k, precision):
     ref = np.max(np.abs(ev.max(axis=1) / ev.min(axis=1)))
     # the smallest eigenvalue carries an FP64 error of ~||Sigma|| eps in any solver
     assert abs(c / ref - 1) <= max(1e-9, 100 * ref * np.finfo(float).eps), (c, ref)
+
+
+def test_illcond_d256_fp64_matches_oracle(gpu_lib, oracle):
+    """The ill-conditioned d = 256 workload (eigenvalues log-spaced over
+    [1e-3, 1e3], condition 1e6) at reduced N and K: FP64 sweeps against the
+    oracle, run like the reference with the condition check off (-S)."""
+    n, d, k = 1 << 14, 256, 4
+    X, info = synth.em_illcond(seed=5, n=n, d=d, k=k)
+    init = (info["weights"], info["means"] + 0.1, info["covs"] * 1.05)
+    ref = oracle.em_train(X, *init, 3, eps=0.0, abort_thr=1e12)
+    with CudaMatrixEM(d, n, k, precision="fp64") as em:
+        em.SetParameters(3, 0.0, 1e12)
+        G = GaussianMixture(*init)
+        em.Train(X, G)
+        ll = em.logl_trace
+        cond = em.FindLargestConditionNumber()
+    np.testing.assert_allclose(ll, ref["logl"], rtol=1e-10)
+    np.testing.assert_allclose(G.means, ref["mu"], rtol=1e-7, atol=1e-8)
+    assert 1e5 < cond < 1e7
+    with pytest.raises(Exception, match="mixed precision"):
+        CudaMatrixEM(d, n, k, precision="mixed")
