@@ -7,5 +7,6 @@ classes, the .bin / .cmp file formats and seeded synthetic workloads.
 """
 from .em import CudaMatrixEM, GaussianMixture  # noqa: F401
 from .kmeans import CudaKMA  # noqa: F401
+from .batch import CudaBatchEM  # noqa: F401
 
-__all__ = ["CudaMatrixEM", "GaussianMixture", "CudaKMA"]
+__all__ = ["CudaMatrixEM", "GaussianMixture", "CudaKMA", "CudaBatchEM"]

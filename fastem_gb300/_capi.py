@@ -33,6 +33,10 @@ EXPORTS = [
     "fem_em_posterior_correlation",
     "fem_em_get_factors", "fem_em_timing_reset", "fem_em_timing_get", "fem_em_timing_total",
     "fem_em_timing_covariance",
+    "fem_em_batch_create", "fem_em_batch_destroy", "fem_em_batch_set_parameters",
+    "fem_em_batch_upload", "fem_em_batch_upload_packed", "fem_em_batch_set_params",
+    "fem_em_batch_get_params", "fem_em_batch_train", "fem_em_batch_trace",
+    "fem_em_batch_fail_component", "fem_em_batch_timing_enable", "fem_em_batch_timing",
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
@@ -103,6 +107,18 @@ def lib():
         "fem_em_timing_get": ([P, P, P, P, P], i32),
         "fem_em_timing_total": ([P, P, P], i32),
         "fem_em_timing_covariance": ([P, P], i32),
+        "fem_em_batch_create": ([i32, P, P, P, ctypes.POINTER(EmConfig), pP], i32),
+        "fem_em_batch_destroy": ([P], None),
+        "fem_em_batch_set_parameters": ([P, i32, f64, f64, f64], i32),
+        "fem_em_batch_upload": ([P, i32, P, i64], i32),
+        "fem_em_batch_upload_packed": ([P, P], i32),
+        "fem_em_batch_set_params": ([P, i32, P, P, P], i32),
+        "fem_em_batch_get_params": ([P, i32, P, P, P], i32),
+        "fem_em_batch_train": ([P, i32, P, P, P], i32),
+        "fem_em_batch_trace": ([P, i32, P, P, i32], i32),
+        "fem_em_batch_fail_component": ([P, i32, P], i32),
+        "fem_em_batch_timing_enable": ([P, i32], i32),
+        "fem_em_batch_timing": ([P, P, P, P], i32),
         "fem_km_config_default": ([ctypes.POINTER(KmConfig)], None),
         "fem_km_create": ([i32, i64, i32, ctypes.POINTER(KmConfig), pP], i32),
         "fem_km_destroy": ([P], None),

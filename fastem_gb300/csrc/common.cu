@@ -2,6 +2,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "fem_internal.cuh"
@@ -15,6 +18,22 @@ void set_error(const char *fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(g_err, sizeof(g_err), fmt, ap);
   va_end(ap);
+}
+
+static std::mutex g_smem_mu;
+static std::map<std::pair<const void *, int>, int> g_smem_limit;
+
+cudaError_t allow_dyn_smem(const void *func, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  int &cur = g_smem_limit[{func, dev}];
+  if ((int)bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = (int)bytes;
+  return e;
 }
 
 static int g_sms = 0;

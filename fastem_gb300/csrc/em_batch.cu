@@ -1,0 +1,1297 @@
+// em_batch.cu -- many independent mixture fits trained together on one GPU.
+//
+// Each fit follows EMAlgorithm::TrainNoCopy (EM2/EMAlgorithm.cpp:139-191)
+// with the SimpleMatrixEM sweep (EM2/MatrixEM.cpp:275-378) on its own data,
+// parameters, convergence test and failure status, exactly as one
+// fem_em_train call would; what changes is the schedule.  Every kernel of a
+// sweep covers all fits that are still active, so a batch of small fits costs
+// a handful of launches per sweep rather than a handful per fit, and the host
+// waits on the device only every kBatchSyncEvery sweeps (to stop early once
+// every fit has converged or failed).
+//
+// Precision: FP32 on CUDA cores for the E-step, means and covariance sums
+// (the fem_em FP32 form); FP64 for the per-item partial sums, the reductions,
+// the Cholesky factors, log-determinants and LogL.
+//
+// Shapes: d <= 32, k <= 64, n < 2^31 per fit.  A fit's dimension class
+// D in {4, 8, 16, 32} is the next power of two >= max(d, 4); kernels are
+// compiled per class and a fit with d < D is computed with zero padding.
+//
+// Layout in HBM: the fits' rows are packed one fit after another (each fit
+// starting on a 16-byte boundary); posteriors are component-major per fit
+// (k x n); W_j = L_j^-1 is stored as a lower triangle whose rows are padded
+// to multiples of 4 floats so the E-step reads it with 16-byte loads.
+//
+// Work items are built on the host when the batch is created (the shapes
+// are fixed): E-step items of 128 P points, means items of kBMChunk points,
+// covariance items of kBCChunk points x one range of <= 256 (component,
+// TB x TB block) units.  Item lists are grouped by dimension class; each
+// class is one launch per phase.
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "em_factor.cuh"
+#include "fem_internal.cuh"
+
+namespace fem {
+namespace {
+
+constexpr int kBMaxD = 32;
+constexpr int kBMaxK = 64;
+constexpr int kBEThreads = 128;
+constexpr int kBMThreads = 128;
+constexpr int kBCThreads = 256;
+constexpr int kBFThreads = 256;
+constexpr int kBMChunk = 2048;   // points per means item
+constexpr int kBCChunk = 4096;   // points per covariance item
+constexpr int kBMTile = 32;      // points staged per means tile
+constexpr int kBCTile = 16;      // points staged per covariance tile
+constexpr int kBatchSyncEvery = 8;
+constexpr int kClasses = 4;      // D = 4, 8, 16, 32
+
+// padded lower triangle: row kk holds kk + 1 entries in 4 * ceil((kk + 1) / 4) floats
+__host__ __device__ constexpr int tri_row(int kk) { return 4 * ((kk + 4) / 4); }
+__host__ __device__ constexpr int tri_off(int kk) {
+  int s = 0;
+  for (int r = 0; r < kk; r++) s += tri_row(r);
+  return s;
+}
+__host__ __device__ constexpr int class_tb(int D) { return D >= 16 ? 8 : 4; }
+__host__ __device__ constexpr int class_nblk(int D) { return (D / class_tb(D)) * (D / class_tb(D) + 1) / 2; }
+int class_of(int d) { return d <= 4 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : 3; }
+int class_dim(int c) { return 4 << c; }
+
+// device descriptor of one fit
+struct BFit {
+  const float *X;        // n x d rows
+  float *R;              // k x n, component-major
+  int64_t n;
+  int d, k, D;
+  int nug;               // covariance unit ranges: ceil(k nblk / 256)
+  int e_first, e_count;  // E-step items (global indices)
+  int m_first, m_count;  // means items
+  int64_t m_part;        // first means partial (doubles): m_count blocks of k (D + 4)
+  int c_chunks;          // covariance chunks (items = c_chunks x nug)
+  int64_t c_part;        // first covariance partial; chunk stride c_stride
+  int64_t c_stride;
+  double *pi, *mu, *sigma, *psum, *logc;   // k, k d, k d d, k, k
+  float *muT, *WT, *logcT;                 // k D, k tri(D), k
+};
+
+// per-fit training state
+struct BState {
+  int active;                 // still sweeping
+  int status;                 // FEM_OK or the error that stopped the fit
+  int iters;                  // EMAlgorithm's IterCounter
+  int chol_failed;            // first failing component of this sweep (INT_MAX: none)
+  unsigned long long cond;    // largest condition number of this sweep (bits of a double >= 0)
+  double logl, prev;
+  int fail_comp;
+  int pad;
+};
+
+struct EItem { int fit, p0; };
+struct MItem { int fit, p0, p1; int64_t part; };
+struct CItem { int fit, p0, p1, u0, u1; int64_t part; };
+
+__device__ __forceinline__ double bwarp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+// deterministic block sum, result in thread 0
+template <int NT>
+__device__ double bblock_sum(double v, double *red) {
+  v = bwarp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; i++) s += red[i];
+  return s;
+}
+
+__device__ __forceinline__ void blse_push(float l, float &mx, float &se) {
+  if (l > mx) {
+    se = se * expf(mx - l) + 1.f;
+    mx = l;
+  } else if (l > -INFINITY) {
+    se += expf(l - mx);
+  }
+}
+
+// s_p += ||row KK of W . t_p||^2 for rows KK.. D-1 of a padded lower
+// triangle W, P centred points; rows by compile-time recursion so every
+// column bound is a constant, two interleaved accumulators per row for
+// instruction-level parallelism
+template <int D, int P, int KK>
+__device__ __forceinline__ void tri_rows(const float (&t)[P][D], const float *__restrict__ w, float (&s)[P]) {
+  float y0[P], y1[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) y0[p] = 0.f, y1[p] = 0.f;
+  const float *wr = w + tri_off(KK);
+#pragma unroll
+  for (int m4 = 0; m4 <= KK / 4; m4++) {
+    const float4 wv = *reinterpret_cast<const float4 *>(wr + 4 * m4);
+    const float we[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      if (4 * m4 + e <= KK) {
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+          if (m4 & 1) y1[p] = fmaf(t[p][4 * m4 + e], we[e], y1[p]);
+          else y0[p] = fmaf(t[p][4 * m4 + e], we[e], y0[p]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    const float y = y0[p] + y1[p];
+    s[p] = fmaf(y, y, s[p]);
+  }
+  if constexpr (KK + 1 < D) tri_rows<D, P, KK + 1>(t, w, s);
+}
+
+// s_p = ||W t_p||^2
+template <int D, int P>
+__device__ __forceinline__ void tri_norms(const float (&t)[P][D], const float *__restrict__ w, float (&s)[P]) {
+#pragma unroll
+  for (int p = 0; p < P; p++) s[p] = 0.f;
+  tri_rows<D, P, 0>(t, w, s);
+}
+
+// ================================================================ E-step
+// MatrixEMBase::BlockDensities + PostProcessDensityMatrix
+// (EM2/MatrixEM.cpp:39-51,69-81) for one item: 128 P points of one fit.
+// The item's rows are staged once in shared memory, transposed (a column of
+// 128 P values per dimension, stride kBEXs: conflict-free stores and reads).
+// Components are staged kc at a time; per component each thread centres its
+// P points on the mean, forms ||W_j (x - mu_j)||^2, writes l_ij to R and
+// keeps an online log-sum-exp; a second pass turns l_ij into
+// exp(l_ij - LSE_i).
+constexpr int kBEP = 4;                          // points per thread
+constexpr int kBEPoints = kBEThreads * kBEP;     // points per item
+constexpr int kBEXs = kBEPoints + 1;             // transposed row stride (floats)
+
+template <int D>
+constexpr size_t estep_smem() { return (size_t)D * kBEXs * sizeof(float); }
+
+template <int D, int P>
+__global__ void __launch_bounds__(kBEThreads)
+k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const EItem *__restrict__ items,
+          double *__restrict__ epart) {
+  static_assert(P == kBEP, "points per thread");
+  constexpr int TRI = tri_off(D);
+  constexpr int KC = D >= 32 ? 8 : 16;
+  extern __shared__ __align__(16) float sXt[];   // D x kBEXs
+  __shared__ __align__(16) float sW[KC * TRI];
+  __shared__ __align__(16) float smu[KC * D];
+  __shared__ float slc[KC];
+  __shared__ double red[kBEThreads / 32];
+  const EItem item = items[blockIdx.x];
+  if (!state[item.fit].active) return;
+  const BFit &F = fits[item.fit];
+  const float *__restrict__ X = F.X;
+  float *__restrict__ R = F.R;
+  const int64_t n = F.n;
+  const int d = F.d, K = F.k, tid = threadIdx.x;
+  const int npts = (int)min((int64_t)kBEPoints, n - item.p0);
+  // rows -> transposed columns (zero past the last point and past column d)
+  if (d == D) {
+    const float4 *src = reinterpret_cast<const float4 *>(X + (size_t)item.p0 * D);
+    for (int e = tid; e < kBEPoints * D / 4; e += kBEThreads) {
+      const int pt = (4 * e) / D, q = (4 * e) % D;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (pt < npts) v = src[e];
+      sXt[(q + 0) * kBEXs + pt] = v.x;
+      sXt[(q + 1) * kBEXs + pt] = v.y;
+      sXt[(q + 2) * kBEXs + pt] = v.z;
+      sXt[(q + 3) * kBEXs + pt] = v.w;
+    }
+  } else {
+    const float *src = X + (size_t)item.p0 * d;
+    for (int e = tid; e < kBEPoints * D; e += kBEThreads) {
+      const int pt = e / D, q = e - pt * D;
+      sXt[q * kBEXs + pt] = (pt < npts && q < d) ? src[(size_t)pt * d + q] : 0.f;
+    }
+  }
+  int64_t idx[P];
+  bool valid[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    idx[p] = (int64_t)item.p0 + tid + p * kBEThreads;
+    valid[p] = idx[p] < n;
+  }
+  float mx[P], se[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) mx[p] = -INFINITY, se[p] = 0.f;
+  for (int j0 = 0; j0 < K; j0 += KC) {
+    const int kc = min(KC, K - j0);
+    __syncthreads();
+    {
+      const float4 *src = reinterpret_cast<const float4 *>(F.WT + (size_t)j0 * TRI);
+      float4 *dst = reinterpret_cast<float4 *>(sW);
+      for (int e = tid; e < kc * TRI / 4; e += kBEThreads) dst[e] = src[e];
+      for (int e = tid; e < kc * D; e += kBEThreads) smu[e] = F.muT[(size_t)j0 * D + e];
+      if (tid < kc) slc[tid] = F.logcT[j0 + tid];
+    }
+    __syncthreads();
+    for (int jj = 0; jj < kc; jj++) {
+      const float *m = smu + jj * D;
+      float t[P][D];
+#pragma unroll
+      for (int q = 0; q < D; q++) {
+        const float mq = m[q];
+#pragma unroll
+        for (int p = 0; p < P; p++) t[p][q] = sXt[q * kBEXs + tid + p * kBEThreads] - mq;
+      }
+      float s[P];
+      tri_norms<D, P>(t, sW + jj * TRI, s);
+      const float lc = slc[jj];
+      float *Rj = R + (size_t)(j0 + jj) * n;
+#pragma unroll
+      for (int p = 0; p < P; p++) {
+        const float l = lc - 0.5f * s[p];
+        if (valid[p]) Rj[idx[p]] = l;
+        blse_push(l, mx[p], se[p]);
+      }
+    }
+  }
+  double v = 0.0;
+  float lse[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    lse[p] = mx[p] + logf(se[p]);
+    if (valid[p]) v += (double)lse[p];
+  }
+  for (int j = 0; j < K; j++) {
+    float *Rj = R + (size_t)j * n;
+#pragma unroll
+    for (int p = 0; p < P; p++)
+      if (valid[p]) Rj[idx[p]] = expf(Rj[idx[p]] - lse[p]);
+  }
+  const double sum = bblock_sum<kBEThreads>(v, red);
+  if (tid == 0) epart[blockIdx.x] = sum;
+}
+
+// ======================================================= M-step: means
+// SimpleMatrixEM::doMStep means part (EM2/MatrixEM.cpp:319-343) for one item:
+// sums_j[c] = sum_i r_ij [x_i | 1][c] over the item's points, as a K x (D+4)
+// block of FP64 partials (column D holds PosteriorSum_j).  Threads own 4 x 4
+// micro-tiles of (component, column); when there are fewer micro-tiles than
+// threads, point groups split each tile's points and are summed at the end.
+// Tiles are loaded into registers one tile ahead.  FP32 sums over the item.
+template <int D>
+__global__ void __launch_bounds__(kBMThreads)
+k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const MItem *__restrict__ items,
+          double *__restrict__ mpart) {
+  constexpr int XC = D + 4, NQB = XC / 4, SR = kBMaxK + 1, TP = kBMTile;
+  constexpr int UPT = (kBMaxK / 4 * NQB + kBMThreads - 1) / kBMThreads;
+  constexpr int XPT = (TP * XC + kBMThreads - 1) / kBMThreads;
+  constexpr int RPT = (kBMaxK * TP + kBMThreads - 1) / kBMThreads;
+  static_assert(TP * SR >= kBMThreads * 16, "group reduction buffer");
+  __shared__ __align__(16) float sX[TP * XC];
+  __shared__ __align__(16) float sR[TP * SR];
+  const MItem item = items[blockIdx.x];
+  if (!state[item.fit].active) return;
+  const BFit &F = fits[item.fit];
+  const float *__restrict__ X = F.X;
+  const float *__restrict__ R = F.R;
+  const int64_t n = F.n;
+  const int d = F.d, K = F.k, tid = threadIdx.x;
+  const int K4 = (K + 3) & ~3, nmt = (K4 / 4) * NQB;
+  const bool grouped = nmt <= kBMThreads;
+  const int UG = grouped ? (nmt + 31) & ~31 : kBMThreads;
+  const int MG = grouped ? kBMThreads / UG : 1;
+  const int g = grouped ? tid / UG : 0;
+  const bool gok = g < MG;
+  int mt[UPT];
+#pragma unroll
+  for (int u = 0; u < UPT; u++) mt[u] = grouped ? (u == 0 ? tid % UG : nmt) : tid + u * kBMThreads;
+  float xr[XPT], rr[RPT];
+  auto fetch = [&](int t0) {
+    const int tp = min(TP, item.p1 - t0);
+#pragma unroll
+    for (int u = 0; u < XPT; u++) {
+      const int e = tid + u * kBMThreads, p = e / XC, c = e - p * XC;
+      float v = 0.f;
+      if (e < TP * XC && p < tp) v = c < d ? X[(size_t)(t0 + p) * d + c] : (c == D ? 1.f : 0.f);
+      xr[u] = v;
+    }
+#pragma unroll
+    for (int u = 0; u < RPT; u++) {
+      const int e = tid + u * kBMThreads, j = e / TP, p = e - j * TP;
+      rr[u] = (j < K && p < tp) ? R[(size_t)j * n + t0 + p] : 0.f;
+    }
+  };
+  fetch(item.p0);
+  float acc[UPT][4][4];
+#pragma unroll
+  for (int u = 0; u < UPT; u++)
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) acc[u][a][b] = 0.f;
+  for (int t0 = item.p0; t0 < item.p1; t0 += TP) {
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < XPT; u++) {
+      const int e = tid + u * kBMThreads;
+      if (e < TP * XC) sX[e] = xr[u];
+    }
+#pragma unroll
+    for (int u = 0; u < RPT; u++) {
+      const int e = tid + u * kBMThreads, j = e / TP, p = e - j * TP;
+      if (j < K4) sR[p * SR + j] = rr[u];
+    }
+    __syncthreads();
+    if (t0 + TP < item.p1) fetch(t0 + TP);
+    if (gok) {
+#pragma unroll
+      for (int u = 0; u < UPT; u++) {
+        if (mt[u] < nmt) {
+          const int jb = mt[u] / NQB, qb = mt[u] - jb * NQB;
+          for (int p = g; p < TP; p += MG) {
+            const float *rp = sR + p * SR + 4 * jb;
+            const float4 xv = *reinterpret_cast<const float4 *>(sX + p * XC + 4 * qb);
+            const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+              const float r = rp[a];
+#pragma unroll
+              for (int b = 0; b < 4; b++) acc[u][a][b] = fmaf(r, xs[b], acc[u][a][b]);
+            }
+          }
+        }
+      }
+    }
+  }
+  if (MG > 1) {
+    // point groups 1.. hand their sums to group 0 (in group order)
+    float *red = sR;
+    __syncthreads();
+    if (gok && g > 0 && mt[0] < nmt)
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) red[((g - 1) * UG + mt[0]) * 16 + a * 4 + b] = acc[0][a][b];
+    __syncthreads();
+    if (g == 0 && mt[0] < nmt)
+      for (int gg = 1; gg < MG; gg++)
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int b = 0; b < 4; b++) acc[0][a][b] += red[((gg - 1) * UG + mt[0]) * 16 + a * 4 + b];
+  }
+  if (g != 0) return;
+  double *o = mpart + item.part;
+#pragma unroll
+  for (int u = 0; u < UPT; u++) {
+    if (mt[u] < nmt) {
+      const int jb = mt[u] / NQB, qb = mt[u] - jb * NQB;
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        const int j = 4 * jb + a;
+        if (j < K)
+#pragma unroll
+          for (int b = 0; b < 4; b++) o[(size_t)j * XC + 4 * qb + b] = (double)acc[u][a][b];
+      }
+    }
+  }
+}
+
+// PosteriorSum, Means = MeanSums / PosteriorSum, Probs = PosteriorSum / N
+// (EM2/MatrixEM.cpp:341-343,375) and LogL = sum_i LSE_i, one CTA per fit;
+// partials summed in item order.
+template <int NT>
+__global__ void __launch_bounds__(NT)
+k_b_final_means(const BFit *__restrict__ fits, BState *__restrict__ state, const double *__restrict__ epart,
+                const double *__restrict__ mpart) {
+  __shared__ double red[NT / 32];
+  const int f = blockIdx.x, tid = threadIdx.x;
+  if (!state[f].active) return;
+  const BFit &F = fits[f];
+  const int K = F.k, d = F.d, D = F.D, XC = D + 4;
+  double v = 0.0;
+  for (int e = tid; e < F.e_count; e += NT) v += epart[F.e_first + e];
+  const double ll = bblock_sum<NT>(v, red);
+  if (tid == 0) state[f].logl = ll;
+  const double *mp = mpart + F.m_part;
+  const size_t stride = (size_t)K * XC;
+  for (int j = tid; j < K; j += NT) {
+    double s = 0.0;
+    for (int c = 0; c < F.m_count; c++) s += mp[c * stride + (size_t)j * XC + D];
+    F.psum[j] = s;
+    F.pi[j] = s / (double)F.n;
+  }
+  __syncthreads();
+  for (int e = tid; e < K * D; e += NT) {
+    const int j = e / D, q = e - j * D;
+    if (q < d) {
+      double s = 0.0;
+      for (int c = 0; c < F.m_count; c++) s += mp[c * stride + (size_t)j * XC + q];
+      const double m = s / F.psum[j];
+      F.mu[(size_t)j * d + q] = m;
+      F.muT[e] = (float)m;
+    } else {
+      F.muT[e] = 0.f;
+    }
+  }
+}
+
+// ================================================== M-step: covariances
+// MatrixEMBase::ComputeWeightedTempDataset + BlockCovariances
+// (EM2/MatrixEM.cpp:53-67,90-99) for one item: z = sqrt(r_ij) (x_i - mu_j)
+// around the new means, CovSum_j += z z^T over the upper block triangle.
+// A unit is one TB x TB block of one component; the item's units
+// [u0, u1) take UG = roundup32(u1 - u0) threads and the CTA's 256 / UG
+// point groups split each tile's points.  Per tile of kBCTile points the x
+// rows and sqrt(r) are staged in shared memory (loaded into registers one
+// tile ahead, so the loads overlap the previous tile's work), z is built
+// there for the item's components, then each unit accumulates its block.
+// FP32 sums over the item's points; each (group, unit) writes its TB x TB
+// block as FP64 partials.
+template <int D>
+struct CovGeom {
+  static constexpr int TB = class_tb(D), NB = D / TB, NBLK = class_nblk(D);
+  static constexpr int ZP = D + 4;                                   // z / x row pitch (floats)
+  static constexpr int CJMAX = kBMaxK < 256 / NBLK + 2 ? kBMaxK : 256 / NBLK + 2;
+  static constexpr int ZCS = kBCTile * ZP + 4;                       // z stride per component (bank skew)
+  static constexpr int XT = kBCTile * D;                             // x tile values
+  static constexpr int XPT = (XT + kBCThreads - 1) / kBCThreads;
+  static constexpr int RPT = (CJMAX * kBCTile + kBCThreads - 1) / kBCThreads;
+  // smem floats: mu (CJ x ZP), x tile (TP x ZP), w (CJ x TP), z (CJ x ZCS)
+  static constexpr size_t floats(int cj) {
+    return (size_t)cj * ZP + (size_t)kBCTile * ZP + (((size_t)cj * kBCTile + 3) & ~(size_t)3) + (size_t)cj * ZCS;
+  }
+};
+
+template <int D>
+__global__ void __launch_bounds__(kBCThreads, 1)
+k_b_cov(const BFit *__restrict__ fits, const BState *__restrict__ state, const CItem *__restrict__ items,
+        double *__restrict__ cpart) {
+  using G = CovGeom<D>;
+  constexpr int TB = G::TB, NB = G::NB, NBLK = G::NBLK, ZP = G::ZP, ZCS = G::ZCS, TP = kBCTile;
+  extern __shared__ __align__(16) float csm[];
+  const CItem item = items[blockIdx.x];
+  if (!state[item.fit].active) return;
+  const BFit &F = fits[item.fit];
+  const float *__restrict__ X = F.X;
+  const float *__restrict__ R = F.R;
+  const int64_t n = F.n;
+  const int d = F.d, tid = threadIdx.x;
+  const int nunits = item.u1 - item.u0;
+  const int UG = (nunits + 31) & ~31, NG = kBCThreads / UG;
+  const int ul = tid % UG, g = tid / UG;
+  const bool act = ul < nunits && g < NG;
+  const int j_lo = item.u0 / NBLK, j_hi = (item.u1 - 1) / NBLK, CJ = j_hi - j_lo + 1;
+  float *smu = csm;                                   // CJ x ZP
+  float *sx = smu + (size_t)CJ * ZP;                  // TP x ZP
+  float *sw = sx + (size_t)TP * ZP;                   // CJ x TP
+  float *sZ = sw + (((size_t)CJ * TP + 3) & ~(size_t)3);   // CJ x ZCS
+  int cj = 0, bi = 0, bj = 0;
+  if (act) {
+    const int unit = item.u0 + ul;
+    const int j = unit / NBLK;
+    int b = unit - j * NBLK;
+    while (b >= NB - bi) {
+      b -= NB - bi;
+      bi++;
+    }
+    bj = bi + b;
+    cj = j - j_lo;
+  }
+  for (int e = tid; e < CJ * ZP; e += kBCThreads) {
+    const int jj = e / ZP, q = e - jj * ZP;
+    smu[e] = q < D ? F.muT[(size_t)(j_lo + jj) * D + q] : 0.f;
+  }
+  // register prefetch of one tile's x values and posteriors
+  float xr[G::XPT], rr[G::RPT];
+  auto fetch = [&](int t0) {
+    const int tp = min(TP, item.p1 - t0);
+#pragma unroll
+    for (int u = 0; u < G::XPT; u++) {
+      const int e = tid + u * kBCThreads, p = e / D, q = e - p * D;
+      xr[u] = (e < G::XT && p < tp && q < d) ? X[(size_t)(t0 + p) * d + q] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < G::RPT; u++) {
+      const int e = tid + u * kBCThreads, jj = e / TP, p = e - jj * TP;
+      rr[u] = (jj < CJ && p < tp) ? R[(size_t)(j_lo + jj) * n + t0 + p] : 0.f;
+    }
+  };
+  fetch(item.p0);
+  float acc[TB][TB];
+#pragma unroll
+  for (int a = 0; a < TB; a++)
+#pragma unroll
+    for (int b = 0; b < TB; b++) acc[a][b] = 0.f;
+  for (int t0 = item.p0; t0 < item.p1; t0 += TP) {
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < G::XPT; u++) {
+      const int e = tid + u * kBCThreads, p = e / D, q = e - p * D;
+      if (e < G::XT) sx[p * ZP + q] = xr[u];
+    }
+#pragma unroll
+    for (int u = 0; u < G::RPT; u++) {
+      const int e = tid + u * kBCThreads;
+      if (e < CJ * TP) sw[e] = sqrtf(rr[u]);
+    }
+    __syncthreads();
+    if (t0 + TP < item.p1) fetch(t0 + TP);
+    for (int e = tid; e < CJ * TP * (D / 4); e += kBCThreads) {
+      const int row = e / (D / 4), q4 = e - row * (D / 4);
+      const int jj = row / TP, p = row - jj * TP;
+      const float w = sw[row];
+      const float4 xv = *reinterpret_cast<const float4 *>(sx + p * ZP + 4 * q4);
+      const float4 mv = *reinterpret_cast<const float4 *>(smu + jj * ZP + 4 * q4);
+      float4 z;
+      z.x = w * (xv.x - mv.x);
+      z.y = w * (xv.y - mv.y);
+      z.z = w * (xv.z - mv.z);
+      z.w = w * (xv.w - mv.w);
+      *reinterpret_cast<float4 *>(sZ + (size_t)jj * ZCS + p * ZP + 4 * q4) = z;
+    }
+    __syncthreads();
+    if (act) {
+      // two points per step (p, p + NG): both rows' loads are issued before the FMAs
+      const float *zb = sZ + (size_t)cj * ZCS;
+      for (int p = g; p < TP; p += 2 * NG) {
+        const bool two = p + NG < TP;
+        float va[2][TB], vb[2][TB];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const float *zr = zb + (two ? p + h * NG : p) * ZP;
+#pragma unroll
+          for (int a4 = 0; a4 < TB / 4; a4++) {
+            const float4 u = *reinterpret_cast<const float4 *>(zr + bi * TB + 4 * a4);
+            const float4 v = *reinterpret_cast<const float4 *>(zr + bj * TB + 4 * a4);
+            va[h][4 * a4 + 0] = u.x, va[h][4 * a4 + 1] = u.y, va[h][4 * a4 + 2] = u.z, va[h][4 * a4 + 3] = u.w;
+            vb[h][4 * a4 + 0] = v.x, vb[h][4 * a4 + 1] = v.y, vb[h][4 * a4 + 2] = v.z, vb[h][4 * a4 + 3] = v.w;
+          }
+        }
+        if (!two)
+#pragma unroll
+          for (int a = 0; a < TB; a++) va[1][a] = 0.f;
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+#pragma unroll
+          for (int a = 0; a < TB; a++)
+#pragma unroll
+            for (int b = 0; b < TB; b++) acc[a][b] = fmaf(va[h][a], vb[h][b], acc[a][b]);
+      }
+    }
+  }
+  if (act) {
+    double *o = cpart + item.part + ((size_t)g * nunits + ul) * (TB * TB);
+#pragma unroll
+    for (int a = 0; a < TB; a++)
+#pragma unroll
+      for (int b = 0; b < TB; b++) o[a * TB + b] = (double)acc[a][b];
+  }
+}
+
+// partial-block geometry of one covariance unit range (shared by host and device)
+__host__ __device__ inline void unit_range(int k, int D, int ug, int *u0, int *u1, int *ng) {
+  const int total = k * class_nblk(D);
+  *u0 = ug * 256;
+  *u1 = min(total, *u0 + 256);
+  const int UG = (*u1 - *u0 + 31) & ~31;
+  *ng = 256 / UG;
+}
+
+// ======================================================= factorisation
+// Covs_j = CovSum_j / PosteriorSum_j (EM2/MatrixEM.cpp:370-373) from the
+// covariance partials (when `reduce`), then RegularizeCovariances +
+// NormalDensity::Init + CalcLogCoeffs (EM2/EMAlgorithm.cpp:237-244,
+// EM2/NormalDensity.cpp:43-65, EM2/MatrixEM.cpp:83-87) in FP64, and with
+// `svd` the condition number (EM2/NormalDensity.cpp:67-71).  One CTA per
+// (fit, component); the factor lives in shared memory.
+__global__ void __launch_bounds__(kBFThreads)
+k_b_factor(const BFit *__restrict__ fits, BState *__restrict__ state, const int2 *__restrict__ comps,
+           const double *__restrict__ cpart, double reg, int reduce, int svd) {
+  __shared__ double sA[kBMaxD * kBMaxD];
+  __shared__ double sWi[kBMaxD * kBMaxD];
+  const int2 fc = comps[blockIdx.x];
+  const int f = fc.x, j = fc.y, tid = threadIdx.x;
+  if (!state[f].active) return;
+  const BFit &F = fits[f];
+  const int d = F.d, D = F.D, K = F.k;
+  double *S = F.sigma + (size_t)j * d * d;
+  if (reduce) {
+    const int TB = class_tb(D), NB = D / TB, NBLK = class_nblk(D), per = TB * TB;
+    const double inv = 1.0 / F.psum[j];
+    for (int e = tid; e < NBLK * per; e += kBFThreads) {
+      const int b = e / per, w = e - b * per;
+      int bi = 0, bb = b;
+      while (bb >= NB - bi) {
+        bb -= NB - bi;
+        bi++;
+      }
+      const int bj = bi + bb;
+      const int a = bi * TB + w / TB, c = bj * TB + (w % TB);
+      if (a > c || c >= d) continue;
+      const int unit = j * NBLK + b, ug = unit / 256, ul = unit - ug * 256;
+      int64_t off = 0;
+      int u0 = 0, u1 = 0, ng = 0;
+      for (int q = 0; q < ug; q++) {
+        unit_range(K, D, q, &u0, &u1, &ng);
+        off += (int64_t)ng * (u1 - u0) * per;
+      }
+      unit_range(K, D, ug, &u0, &u1, &ng);
+      const int nu = u1 - u0;
+      double s = 0.0;
+      for (int ch = 0; ch < F.c_chunks; ch++) {
+        const double *pp = cpart + F.c_part + ch * F.c_stride + off + (size_t)ul * per + w;
+        for (int gg = 0; gg < ng; gg++) s += pp[(size_t)gg * nu * per];
+      }
+      s *= inv;
+      S[(size_t)a * d + c] = s;
+      S[(size_t)c * d + a] = s;
+    }
+    __syncthreads();
+  }
+  if (reg != 0.0) block_regularize(S, d, reg);
+  if (!block_cholesky(S, d, sA)) {
+    if (tid == 0) atomicMin(&state[f].chol_failed, j);
+    return;
+  }
+  block_lower_inverse(sA, d, sWi);
+  if (tid == 0) {
+    const double ld = chol_logdet(sA, d);
+    const double lc = log(F.pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
+    F.logc[j] = lc;
+    F.logcT[j] = (float)lc;
+  }
+  const int TRI = tri_off(D);
+  float *Wt = F.WT + (size_t)j * TRI;
+  for (int e = tid; e < TRI; e += kBFThreads) {
+    int kk = 0, off = 0;
+    while (off + tri_row(kk) <= e) off += tri_row(kk++);
+    const int m = e - off;
+    Wt[e] = (kk < d && m <= kk) ? (float)sWi[kk * d + m] : 0.f;
+  }
+  if (svd) {
+    __syncthreads();
+    for (int e = tid; e < d * d; e += kBFThreads) {
+      const int r = e / d, c = e - r * d;
+      sA[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
+    }
+    __syncthreads();
+    const double cond = block_jacobi_cond(sA, d);
+    if (tid == 0) atomicMax(&state[f].cond, (unsigned long long)__double_as_longlong(cond));
+  }
+}
+
+// the end of one sweep of TrainNoCopy's loop (EM2/EMAlgorithm.cpp:167-185)
+// for every active fit: a failed factorisation or a condition number above
+// AbortThr stops the fit with IterCounter = it; otherwise LogL and e go to
+// the traces and |dL/L| < Eps or MaxSweeps stops it with it + 1.  it = 0 is
+// the factorisation before the first sweep.  One CTA; *nactive counts the
+// fits still sweeping.
+__global__ void __launch_bounds__(1024)
+k_b_sweep_end(BState *__restrict__ state, int nfits, int it, int max_sweeps, double eps, double abort_thr,
+              int svd, double *__restrict__ trace, double *__restrict__ etrace, int cap, int *nactive) {
+  __shared__ double red[32];
+  double cnt = 0.0;
+  for (int f = threadIdx.x; f < nfits; f += 1024) {
+    BState &s = state[f];
+    if (!s.active) continue;
+    if (s.chol_failed != INT_MAX) {
+      s.status = FEM_ERR_CHOLESKY;
+      s.fail_comp = s.chol_failed;
+      s.iters = it;
+      s.active = 0;
+      continue;
+    }
+    if (svd) {
+      const double cond = __longlong_as_double((long long)s.cond);
+      s.cond = 0ull;
+      if (cond > abort_thr) {
+        s.status = FEM_ERR_COND_ABORT;
+        s.iters = it;
+        s.active = 0;
+        continue;
+      }
+    }
+    if (it > 0) {
+      const double logl = s.logl;
+      double e = fabs((logl - s.prev) / logl);
+      if (logl < s.prev) e = 0.0;
+      if (it - 1 < cap) {
+        trace[(size_t)f * cap + it - 1] = logl;
+        etrace[(size_t)f * cap + it - 1] = e;
+      }
+      s.prev = logl;
+      s.iters = it + 1;
+      if (e < eps || it >= max_sweeps) {
+        s.active = 0;
+        continue;
+      }
+    }
+    cnt += 1.0;
+  }
+  const double total = bblock_sum<1024>(cnt, red);
+  if (threadIdx.x == 0) *nactive = (int)total;
+}
+
+}  // namespace
+}  // namespace fem
+
+using namespace fem;
+
+struct fem_em_batch {
+  int nfits = 0;
+  fem_em_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::vector<BFit> hfits;
+  std::vector<char> have_data, have_params;
+  int cap = 0;                      // trace entries per fit
+  // device
+  BFit *fits = nullptr;
+  BState *state = nullptr;
+  float *X = nullptr, *R = nullptr, *muT = nullptr, *WT = nullptr, *logcT = nullptr;
+  double *pi = nullptr, *mu = nullptr, *sigma = nullptr, *psum = nullptr, *logc = nullptr;
+  double *epart = nullptr, *mpart = nullptr, *cpart = nullptr;
+  double *trace = nullptr, *etrace = nullptr;
+  int *nactive = nullptr, *hnactive = nullptr;   // device / pinned host
+  EItem *eitems = nullptr;
+  MItem *mitems = nullptr;
+  CItem *citems = nullptr;
+  int2 *comps = nullptr;
+  int ncomps = 0;
+  int e_beg[kClasses + 1] = {}, m_beg[kClasses + 1] = {}, c_beg[kClasses + 1] = {};
+  size_t c_smem[kClasses] = {};
+  std::vector<BState> hstate;
+  // timing: phase boundaries of the sweeps since the last host sync
+  bool timing = false;
+  cudaEvent_t pev[kBatchSyncEvery][5] = {};
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+  double t_phase[5] = {};           // E-step, means, covariance, factorisation, whole sweep loop
+  int64_t launches = 0, sweeps = 0;
+};
+
+namespace {
+
+int check_batch(fem_em_batch *b) {
+  if (!b) {
+    set_error("null batch handle");
+    return FEM_ERR_BAD_ARG;
+  }
+  return FEM_OK;
+}
+
+int check_fit(fem_em_batch *b, int fit) {
+  FEM_TRY(check_batch(b));
+  if (fit < 0 || fit >= b->nfits) {
+    set_error("fit index %d out of range [0, %d)", fit, b->nfits);
+    return FEM_ERR_BAD_ARG;
+  }
+  return FEM_OK;
+}
+
+void free_batch(fem_em_batch *b) {
+  dfree(b->fits);
+  dfree(b->state);
+  dfree(b->X);
+  dfree(b->R);
+  dfree(b->muT);
+  dfree(b->WT);
+  dfree(b->logcT);
+  dfree(b->pi);
+  dfree(b->mu);
+  dfree(b->sigma);
+  dfree(b->psum);
+  dfree(b->logc);
+  dfree(b->epart);
+  dfree(b->mpart);
+  dfree(b->cpart);
+  dfree(b->trace);
+  dfree(b->etrace);
+  dfree(b->nactive);
+  dfree(b->eitems);
+  dfree(b->mitems);
+  dfree(b->citems);
+  dfree(b->comps);
+  if (b->hnactive) cudaFreeHost(b->hnactive);
+  for (auto &row : b->pev)
+    for (auto &e : row)
+      if (e) cudaEventDestroy(e);
+  if (b->ev_start) cudaEventDestroy(b->ev_start);
+  if (b->ev_end) cudaEventDestroy(b->ev_end);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+template <class T>
+int upload_vec(T **dst, const std::vector<T> &v) {
+  FEM_TRY(dalloc(dst, v.size()));
+  if (!v.empty()) FEM_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return FEM_OK;
+}
+
+
+void mark(fem_em_batch *b, int slot, int phase) {
+  if (b->timing) cudaEventRecord(b->pev[slot][phase], b->stream);
+}
+
+// per-phase device time of the sweeps recorded in event slots [0, pending)
+void collect_timing(fem_em_batch *b, int pending) {
+  float ms = 0.f;
+  for (int s = 0; s < pending; s++)
+    for (int p = 0; p < 4; p++)
+      if (cudaEventElapsedTime(&ms, b->pev[s][p], b->pev[s][p + 1]) == cudaSuccess) b->t_phase[p] += ms;
+}
+
+int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
+  const BFit *fits = b->fits;
+  BState *st = b->state;
+  mark(b, slot, 0);
+  for (int c = 0; c < kClasses; c++) {
+    const int cnt = b->e_beg[c + 1] - b->e_beg[c];
+    if (!cnt) continue;
+    const EItem *it0 = b->eitems + b->e_beg[c];
+    double *ep = b->epart + b->e_beg[c];
+    switch (c) {
+      case 0: k_b_estep<4, kBEP><<<cnt, kBEThreads, estep_smem<4>(), b->stream>>>(fits, st, it0, ep); break;
+      case 1: k_b_estep<8, kBEP><<<cnt, kBEThreads, estep_smem<8>(), b->stream>>>(fits, st, it0, ep); break;
+      case 2: k_b_estep<16, kBEP><<<cnt, kBEThreads, estep_smem<16>(), b->stream>>>(fits, st, it0, ep); break;
+      default: k_b_estep<32, kBEP><<<cnt, kBEThreads, estep_smem<32>(), b->stream>>>(fits, st, it0, ep); break;
+    }
+    FEM_CUDA(cudaGetLastError());
+    b->launches++;
+  }
+  mark(b, slot, 1);
+  for (int c = 0; c < kClasses; c++) {
+    const int cnt = b->m_beg[c + 1] - b->m_beg[c];
+    if (!cnt) continue;
+    const MItem *it0 = b->mitems + b->m_beg[c];
+    switch (c) {
+      case 0: k_b_means<4><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
+      case 1: k_b_means<8><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
+      case 2: k_b_means<16><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
+      default: k_b_means<32><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
+    }
+    FEM_CUDA(cudaGetLastError());
+    b->launches++;
+  }
+  k_b_final_means<128><<<b->nfits, 128, 0, b->stream>>>(fits, st, b->epart, b->mpart);
+  FEM_CUDA(cudaGetLastError());
+  b->launches++;
+  mark(b, slot, 2);
+  for (int c = 0; c < kClasses; c++) {
+    const int cnt = b->c_beg[c + 1] - b->c_beg[c];
+    if (!cnt) continue;
+    const CItem *it0 = b->citems + b->c_beg[c];
+    const size_t sm = b->c_smem[c];
+    switch (c) {
+      case 0: k_b_cov<4><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
+      case 1: k_b_cov<8><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
+      case 2: k_b_cov<16><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
+      default: k_b_cov<32><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
+    }
+    FEM_CUDA(cudaGetLastError());
+    b->launches++;
+  }
+  mark(b, slot, 3);
+  k_b_factor<<<b->ncomps, kBFThreads, 0, b->stream>>>(fits, st, b->comps, b->cpart, b->cfg.reg_coef, 1, svd);
+  FEM_CUDA(cudaGetLastError());
+  k_b_sweep_end<<<1, 1024, 0, b->stream>>>(st, b->nfits, it, b->cfg.max_sweeps, b->cfg.eps, b->cfg.abort_thr, svd,
+                                           b->trace, b->etrace, b->cap, b->nactive);
+  FEM_CUDA(cudaGetLastError());
+  b->launches += 2;
+  mark(b, slot, 4);
+  return FEM_OK;
+}
+
+}  // namespace
+
+extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, const int *k,
+                                   const fem_em_config *cfg, fem_em_batch **out) {
+  if (!out || nfits < 1 || !d || !n || !k) {
+    set_error("fem_em_batch_create: bad arguments");
+    return FEM_ERR_BAD_ARG;
+  }
+  *out = nullptr;
+  fem_em_config c;
+  if (cfg) c = *cfg;
+  else {
+    fem_em_config_default(&c);
+    c.precision = FEM_PREC_FP32;
+  }
+  if (c.precision != FEM_PREC_FP32) {
+    set_error("batched fits run in FP32 on CUDA cores (precision FEM_PREC_FP32)");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  if (c.max_sweeps < 1) {
+    set_error("max_sweeps must be >= 1");
+    return FEM_ERR_BAD_ARG;
+  }
+  for (int f = 0; f < nfits; f++) {
+    if (d[f] < 1 || k[f] < 1 || n[f] < 1) {
+      set_error("fit %d: d, n and k must be positive", f);
+      return FEM_ERR_BAD_ARG;
+    }
+    if (d[f] > kBMaxD || k[f] > kBMaxK || n[f] >= ((int64_t)1 << 31)) {
+      set_error("fit %d: batched fits need d <= %d, k <= %d, n < 2^31 (got d=%d k=%d n=%lld)", f, kBMaxD,
+                kBMaxK, d[f], k[f], (long long)n[f]);
+      return FEM_ERR_UNSUPPORTED;
+    }
+  }
+  FEM_TRY(select_device(c.device));
+  fem_em_batch *b = new (std::nothrow) fem_em_batch;
+  if (!b) {
+    set_error("out of host memory");
+    return FEM_ERR_BAD_ARG;
+  }
+  b->nfits = nfits;
+  b->cfg = c;
+  b->hfits.resize(nfits);
+  b->have_data.assign(nfits, 0);
+  b->have_params.assign(nfits, 0);
+  b->cap = std::min(c.max_sweeps, 4096);
+  int st = FEM_OK;
+  auto fail = [&](int s) {
+    free_batch(b);
+    delete b;
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("stream creation failed");
+    return fail(FEM_ERR_CUDA);
+  }
+  // sizes and offsets
+  int64_t nx = 0, nr = 0, nk = 0, nkd = 0, nkdd = 0, nkD = 0, nkT = 0;
+  std::vector<int64_t> ox(nfits), orr(nfits), ok_(nfits), okd(nfits), okdd(nfits), okD(nfits), okT(nfits);
+  for (int f = 0; f < nfits; f++) {
+    const int D = class_dim(class_of(d[f]));
+    ox[f] = nx, orr[f] = nr, ok_[f] = nk, okd[f] = nkd, okdd[f] = nkdd, okD[f] = nkD, okT[f] = nkT;
+    nx += (n[f] * d[f] + 3) & ~(int64_t)3;
+    nr += n[f] * k[f];
+    nk += k[f];
+    nkd += (int64_t)k[f] * d[f];
+    nkdd += (int64_t)k[f] * d[f] * d[f];
+    nkD += (int64_t)k[f] * D;
+    nkT += (int64_t)k[f] * tri_off(D);
+  }
+  if ((st = dalloc(&b->X, nx)) || (st = dalloc(&b->R, nr)) || (st = dalloc(&b->muT, nkD)) ||
+      (st = dalloc(&b->WT, nkT)) || (st = dalloc(&b->logcT, nk)) || (st = dalloc(&b->pi, nk)) ||
+      (st = dalloc(&b->mu, nkd)) || (st = dalloc(&b->sigma, nkdd)) || (st = dalloc(&b->psum, nk)) ||
+      (st = dalloc(&b->logc, nk)))
+    return fail(st);
+  // work items, grouped by dimension class
+  std::vector<EItem> ei;
+  std::vector<MItem> mi;
+  std::vector<CItem> ci;
+  std::vector<int2> comps;
+  int64_t mp = 0, cp = 0;
+  for (int f = 0; f < nfits; f++) {
+    BFit &F = b->hfits[f];
+    F.X = b->X + ox[f];
+    F.R = b->R + orr[f];
+    F.n = n[f];
+    F.d = d[f];
+    F.k = k[f];
+    F.D = class_dim(class_of(d[f]));
+    F.pi = b->pi + ok_[f];
+    F.mu = b->mu + okd[f];
+    F.sigma = b->sigma + okdd[f];
+    F.psum = b->psum + ok_[f];
+    F.logc = b->logc + ok_[f];
+    F.muT = b->muT + okD[f];
+    F.WT = b->WT + okT[f];
+    F.logcT = b->logcT + ok_[f];
+    for (int j = 0; j < k[f]; j++) comps.push_back(make_int2(f, j));
+  }
+  for (int c = 0; c < kClasses; c++) {
+    b->e_beg[c] = (int)ei.size();
+    b->m_beg[c] = (int)mi.size();
+    b->c_beg[c] = (int)ci.size();
+    int kmax = 0;
+    for (int f = 0; f < nfits; f++) {
+      BFit &F = b->hfits[f];
+      if (class_of(F.d) != c) continue;
+      kmax = std::max(kmax, F.k);
+      const int ep = kBEPoints;
+      F.e_first = (int)ei.size();
+      for (int64_t p = 0; p < F.n; p += ep) ei.push_back(EItem{f, (int)p});
+      F.e_count = (int)ei.size() - F.e_first;
+      F.m_first = (int)mi.size();
+      F.m_part = mp;
+      for (int64_t p = 0; p < F.n; p += kBMChunk) {
+        mi.push_back(MItem{f, (int)p, (int)std::min<int64_t>(F.n, p + kBMChunk), mp});
+        mp += (int64_t)F.k * (F.D + 4);
+      }
+      F.m_count = (int)mi.size() - F.m_first;
+      const int per = class_tb(F.D) * class_tb(F.D);
+      F.nug = (F.k * class_nblk(F.D) + 255) / 256;
+      F.c_part = cp;
+      F.c_stride = 0;
+      for (int ug = 0; ug < F.nug; ug++) {
+        int u0, u1, ng;
+        unit_range(F.k, F.D, ug, &u0, &u1, &ng);
+        F.c_stride += (int64_t)ng * (u1 - u0) * per;
+      }
+      F.c_chunks = 0;
+      for (int64_t p = 0; p < F.n; p += kBCChunk) {
+        int64_t off = cp;
+        for (int ug = 0; ug < F.nug; ug++) {
+          int u0, u1, ng;
+          unit_range(F.k, F.D, ug, &u0, &u1, &ng);
+          ci.push_back(CItem{f, (int)p, (int)std::min<int64_t>(F.n, p + kBCChunk), u0, u1, off});
+          off += (int64_t)ng * (u1 - u0) * per;
+        }
+        cp += F.c_stride;
+        F.c_chunks++;
+      }
+    }
+    const int D = class_dim(c), nblk = class_nblk(D);
+    const int cj = std::max(1, std::min(kmax, 256 / nblk + 2));
+    size_t fl = 0;
+    switch (c) {
+      case 0: fl = CovGeom<4>::floats(cj); break;
+      case 1: fl = CovGeom<8>::floats(cj); break;
+      case 2: fl = CovGeom<16>::floats(cj); break;
+      default: fl = CovGeom<32>::floats(cj); break;
+    }
+    b->c_smem[c] = fl * sizeof(float);
+  }
+  b->e_beg[kClasses] = (int)ei.size();
+  b->m_beg[kClasses] = (int)mi.size();
+  b->c_beg[kClasses] = (int)ci.size();
+  b->ncomps = (int)comps.size();
+  if ((st = upload_vec(&b->eitems, ei)) || (st = upload_vec(&b->mitems, mi)) || (st = upload_vec(&b->citems, ci)) ||
+      (st = upload_vec(&b->comps, comps)) || (st = dalloc(&b->epart, ei.size())) || (st = dalloc(&b->mpart, mp)) ||
+      (st = dalloc(&b->cpart, cp)) || (st = dalloc(&b->state, nfits)) ||
+      (st = dalloc(&b->trace, (size_t)nfits * b->cap)) || (st = dalloc(&b->etrace, (size_t)nfits * b->cap)) ||
+      (st = dalloc(&b->nactive, 1)) || (st = upload_vec(&b->fits, b->hfits)))
+    return fail(st);
+  if (cudaMallocHost((void **)&b->hnactive, sizeof(int)) != cudaSuccess) {
+    set_error("pinned allocation failed");
+    return fail(FEM_ERR_CUDA);
+  }
+  for (auto &row : b->pev)
+    for (auto &e : row)
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        set_error("event creation failed");
+        return fail(FEM_ERR_CUDA);
+      }
+  if (cudaEventCreate(&b->ev_start) != cudaSuccess || cudaEventCreate(&b->ev_end) != cudaSuccess) {
+    set_error("event creation failed");
+    return fail(FEM_ERR_CUDA);
+  }
+  if (allow_dyn_smem(k_b_estep<16, kBEP>, estep_smem<16>()) != cudaSuccess ||
+      allow_dyn_smem(k_b_estep<32, kBEP>, estep_smem<32>()) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov<4>, b->c_smem[0]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov<8>, b->c_smem[1]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov<16>, b->c_smem[2]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov<32>, b->c_smem[3]) != cudaSuccess) {
+    set_error("batched kernels' shared-memory limits could not be raised");
+    return fail(FEM_ERR_CUDA);
+  }
+  b->hstate.resize(nfits);
+  *out = b;
+  return FEM_OK;
+}
+
+extern "C" void fem_em_batch_destroy(fem_em_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->cfg.device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_batch(b);
+  delete b;
+}
+
+extern "C" int fem_em_batch_upload(fem_em_batch *b, int fit, const float *X, int64_t ld) {
+  FEM_TRY(check_fit(b, fit));
+  const BFit &F = b->hfits[fit];
+  if (!X || ld < F.d) {
+    set_error("fem_em_batch_upload: null rows or ld < d");
+    return FEM_ERR_BAD_ARG;
+  }
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  FEM_CUDA(cudaMemcpy2DAsync((void *)F.X, (size_t)F.d * sizeof(float), X, (size_t)ld * sizeof(float),
+                             (size_t)F.d * sizeof(float), (size_t)F.n, cudaMemcpyHostToDevice, b->stream));
+  FEM_CUDA(cudaStreamSynchronize(b->stream));
+  b->have_data[fit] = 1;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_upload_packed(fem_em_batch *b, const float *X) {
+  FEM_TRY(check_batch(b));
+  if (!X) {
+    set_error("fem_em_batch_upload_packed: null rows");
+    return FEM_ERR_BAD_ARG;
+  }
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  const float *src = X;
+  for (int f = 0; f < b->nfits; f++) {
+    const BFit &F = b->hfits[f];
+    FEM_CUDA(cudaMemcpyAsync((void *)F.X, src, (size_t)F.n * F.d * sizeof(float), cudaMemcpyHostToDevice,
+                             b->stream));
+    src += (size_t)F.n * F.d;
+    b->have_data[f] = 1;
+  }
+  FEM_CUDA(cudaStreamSynchronize(b->stream));
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_set_params(fem_em_batch *b, int fit, const double *pi, const double *mu,
+                                       const double *sigma) {
+  FEM_TRY(check_fit(b, fit));
+  if (!pi || !mu || !sigma) {
+    set_error("fem_em_batch_set_params: null argument");
+    return FEM_ERR_BAD_ARG;
+  }
+  const BFit &F = b->hfits[fit];
+  const int k = F.k, d = F.d, D = F.D;
+  std::vector<float> muT((size_t)k * D, 0.f);
+  for (int j = 0; j < k; j++)
+    for (int q = 0; q < d; q++) muT[(size_t)j * D + q] = (float)mu[(size_t)j * d + q];
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  FEM_CUDA(cudaMemcpyAsync(F.pi, pi, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  FEM_CUDA(cudaMemcpyAsync(F.mu, mu, (size_t)k * d * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  FEM_CUDA(cudaMemcpyAsync(F.sigma, sigma, (size_t)k * d * d * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  FEM_CUDA(cudaMemcpyAsync(F.muT, muT.data(), muT.size() * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+  FEM_CUDA(cudaStreamSynchronize(b->stream));
+  b->have_params[fit] = 1;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_get_params(fem_em_batch *b, int fit, double *pi, double *mu, double *sigma) {
+  FEM_TRY(check_fit(b, fit));
+  const BFit &F = b->hfits[fit];
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  if (pi) FEM_CUDA(cudaMemcpyAsync(pi, F.pi, (size_t)F.k * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (mu)
+    FEM_CUDA(cudaMemcpyAsync(mu, F.mu, (size_t)F.k * F.d * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (sigma)
+    FEM_CUDA(cudaMemcpyAsync(sigma, F.sigma, (size_t)F.k * F.d * F.d * sizeof(double), cudaMemcpyDeviceToHost,
+                             b->stream));
+  FEM_CUDA(cudaStreamSynchronize(b->stream));
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_set_parameters(fem_em_batch *b, int max_sweeps, double eps, double abort_thr,
+                                           double reg_coef) {
+  FEM_TRY(check_batch(b));
+  if (max_sweeps < 1) {
+    set_error("max_sweeps must be >= 1");
+    return FEM_ERR_BAD_ARG;
+  }
+  b->cfg.max_sweeps = max_sweeps;
+  b->cfg.eps = eps;
+  b->cfg.abort_thr = abort_thr;
+  b->cfg.reg_coef = reg_coef;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_train(fem_em_batch *b, int svd, int *status, int *iter_counter, double *logl) {
+  FEM_TRY(check_batch(b));
+  for (int f = 0; f < b->nfits; f++)
+    if (!b->have_data[f] || !b->have_params[f]) {
+      set_error("fit %d: train needs an uploaded dataset and parameters", f);
+      return FEM_ERR_STATE;
+    }
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  for (auto &s : b->hstate) {
+    s = BState{};
+    s.active = 1;
+    s.status = FEM_OK;
+    s.chol_failed = INT_MAX;
+    s.prev = -DBL_MAX;
+    s.logl = -DBL_MAX;
+    s.fail_comp = -1;
+  }
+  FEM_CUDA(cudaMemcpyAsync(b->state, b->hstate.data(), b->hstate.size() * sizeof(BState), cudaMemcpyHostToDevice,
+                           b->stream));
+  // factorisation of the initial parameters (the fits' psum is not used)
+  k_b_factor<<<b->ncomps, kBFThreads, 0, b->stream>>>(b->fits, b->state, b->comps, b->cpart, b->cfg.reg_coef, 0,
+                                                      svd);
+  FEM_CUDA(cudaGetLastError());
+  k_b_sweep_end<<<1, 1024, 0, b->stream>>>(b->state, b->nfits, 0, b->cfg.max_sweeps, b->cfg.eps, b->cfg.abort_thr,
+                                           svd, b->trace, b->etrace, b->cap, b->nactive);
+  FEM_CUDA(cudaGetLastError());
+  b->launches += 2;
+  if (b->timing) FEM_CUDA(cudaEventRecord(b->ev_start, b->stream));
+  int pending = 0;
+  for (int it = 1; it <= b->cfg.max_sweeps; it++) {
+    FEM_TRY(launch_sweep(b, it, svd, pending++));
+    b->sweeps++;
+    if (pending == kBatchSyncEvery || it == b->cfg.max_sweeps) {
+      FEM_CUDA(cudaMemcpyAsync(b->hnactive, b->nactive, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+      FEM_CUDA(cudaStreamSynchronize(b->stream));
+      if (b->timing) collect_timing(b, pending);
+      pending = 0;
+      if (*b->hnactive == 0) break;
+    }
+  }
+  if (b->timing) {
+    float ms = 0.f;
+    FEM_CUDA(cudaEventRecord(b->ev_end, b->stream));
+    FEM_CUDA(cudaEventSynchronize(b->ev_end));
+    if (cudaEventElapsedTime(&ms, b->ev_start, b->ev_end) == cudaSuccess) b->t_phase[4] += ms;
+  }
+  FEM_CUDA(cudaMemcpyAsync(b->hstate.data(), b->state, b->hstate.size() * sizeof(BState), cudaMemcpyDeviceToHost,
+                           b->stream));
+  FEM_CUDA(cudaStreamSynchronize(b->stream));
+  int nfail = 0;
+  for (int f = 0; f < b->nfits; f++) {
+    const BState &s = b->hstate[f];
+    if (status) status[f] = s.status;
+    if (iter_counter) iter_counter[f] = s.iters;
+    if (logl) logl[f] = s.logl;
+    nfail += s.status != FEM_OK;
+  }
+  if (nfail) set_error("%d of %d fits stopped with an error (see the per-fit status)", nfail, b->nfits);
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_trace(fem_em_batch *b, int fit, double *logl_trace, double *e_trace, int capacity) {
+  FEM_TRY(check_fit(b, fit));
+  const int m = std::min(capacity, b->cap);
+  FEM_CUDA(cudaSetDevice(b->cfg.device));
+  if (logl_trace && m > 0)
+    FEM_CUDA(cudaMemcpy(logl_trace, b->trace + (size_t)fit * b->cap, (size_t)m * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+  if (e_trace && m > 0)
+    FEM_CUDA(cudaMemcpy(e_trace, b->etrace + (size_t)fit * b->cap, (size_t)m * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_fail_component(fem_em_batch *b, int fit, int *component) {
+  FEM_TRY(check_fit(b, fit));
+  if (!component) {
+    set_error("null output");
+    return FEM_ERR_BAD_ARG;
+  }
+  *component = b->hstate[fit].fail_comp;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_timing_enable(fem_em_batch *b, int on) {
+  FEM_TRY(check_batch(b));
+  b->timing = on != 0;
+  for (double &t : b->t_phase) t = 0.0;
+  b->launches = 0;
+  b->sweeps = 0;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_timing(fem_em_batch *b, double *phase_ms, int64_t *launches, int64_t *sweeps) {
+  FEM_TRY(check_batch(b));
+  if (phase_ms)
+    for (int p = 0; p < 5; p++) phase_ms[p] = b->t_phase[p];
+  if (launches) *launches = b->launches;
+  if (sweeps) *sweeps = b->sweeps;
+  return FEM_OK;
+}

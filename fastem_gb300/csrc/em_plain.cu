@@ -16,6 +16,7 @@
 
 #include "fem_internal.cuh"
 #include "em_kernels.cuh"
+#include "em_factor.cuh"
 
 namespace fem {
 
@@ -160,7 +161,10 @@ __global__ void __launch_bounds__(1024) k_reduce_logl(const double *part, int64_
 // ======================================================= M-step: means
 // SimpleMatrixEM::doMStep means part (EM2/MatrixEM.cpp:319-343):
 // PosteriorSum_j = sum_i r_ij and MeanSums_j = sum_i r_ij x_i per block of
-// rows; each thread owns (component, C-column chunk) units.
+// rows; each thread owns (component, C-column chunk) units.  The last chunk
+// of a row may be partial (C does not divide d): its lanes past column d
+// read staged values of the next row (or the padding after the last one)
+// and are never written out.
 constexpr int kMeanTP = 32;
 
 template <typename T, int C, int UPT>
@@ -168,10 +172,10 @@ __global__ void __launch_bounds__(256)
 k_means_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__restrict__ R,
               double *__restrict__ part, int64_t rows_per_block) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *sX = (float *)smem_raw;                       // TP x d
-  T *sR = (T *)(sX + kMeanTP * d);                     // K x (TP+1)
+  float *sX = (float *)smem_raw;                       // TP x d, then C floats of padding
+  T *sR = (T *)(sX + kMeanTP * d + C);                 // K x (TP+1)
   const int tid = threadIdx.x;
-  const int nch = d / C, units = K * nch;
+  const int nch = (d + C - 1) / C, units = K * nch;
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
   const int64_t r1 = min(n, r0 + rows_per_block);
   T acc[UPT][C], acc1[UPT];
@@ -234,7 +238,8 @@ k_means_plain(const float *__restrict__ X, int64_t n, int d, int K, const T *__r
       double *o = part + ((size_t)blockIdx.x * K + j) * (d + 1);
       if (c == 0) o[0] = dacc1[u];
 #pragma unroll
-      for (int a = 0; a < C; a++) o[1 + c * C + a] = dacc[u][a];
+      for (int a = 0; a < C; a++)
+        if (c * C + a < d) o[1 + c * C + a] = dacc[u][a];
     }
   }
 }
@@ -405,72 +410,14 @@ k_factor(int K, int d, double reg, int regularize, double *__restrict__ sigma,
   double *S = sigma + (size_t)j * d * d;
   double *A = work + (size_t)j * d * d;
   double *Wi = linv + (size_t)j * d * d;
-  __shared__ double s_piv;
-  __shared__ int s_fail;
-  if (regularize && reg != 0.0) {
-    if (tid == 0) {
-      double tr = 0.0;
-      for (int q = 0; q < d; q++) tr += S[(size_t)q * d + q];
-      s_piv = reg * tr / (double)d;
-    }
-    __syncthreads();
-    const double add = s_piv;
-    for (int e = tid; e < d * d; e += nt) {
-      const int r = e / d, c = e - r * d;
-      S[e] = S[e] * (1.0 - reg) + (r == c ? add : 0.0);
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < d * d; e += nt) {
-    const int r = e / d, c = e - r * d;
-    A[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
-  }
-  if (tid == 0) s_fail = 0;
-  __syncthreads();
-  for (int k = 0; k < d; k++) {
-    if (tid == 0) {
-      const double x = A[(size_t)k * d + k];
-      if (!(x > 0.0)) {
-        s_fail = 1;
-      } else {
-        const double l = sqrt(x);
-        A[(size_t)k * d + k] = l;
-        s_piv = l;
-      }
-    }
-    __syncthreads();
-    if (s_fail) break;
-    const double lkk = s_piv;
-    for (int i = k + 1 + tid; i < d; i += nt) A[(size_t)i * d + k] /= lkk;
-    __syncthreads();
-    // trailing update of the lower triangle: A[i][c] -= L[i][k] L[c][k], k < c <= i
-    const int m = d - k - 1;
-    for (int e = tid; e < m * m; e += nt) {
-      const int i = e / m, c = e - i * m;
-      if (c > i) continue;
-      const int gi = k + 1 + i, gc = k + 1 + c;
-      A[(size_t)gi * d + gc] -= A[(size_t)gi * d + k] * A[(size_t)gc * d + k];
-    }
-    __syncthreads();
-  }
-  if (s_fail) {
+  if (regularize && reg != 0.0) block_regularize(S, d, reg);
+  if (!block_cholesky(S, d, A)) {
     if (tid == 0) atomicMin(&st->chol_failed, j);
     return;
   }
-  // W = L^-1, column c by forward substitution (threads own columns)
-  for (int c = tid; c < d; c += nt) {
-    for (int r = 0; r < c; r++) Wi[(size_t)r * d + c] = 0.0;
-    for (int r = c; r < d; r++) {
-      double s = (r == c) ? 1.0 : 0.0;
-      for (int m2 = c; m2 < r; m2++) s -= A[(size_t)r * d + m2] * Wi[(size_t)m2 * d + c];
-      Wi[(size_t)r * d + c] = s / A[(size_t)r * d + r];
-    }
-  }
-  __syncthreads();
+  block_lower_inverse(A, d, Wi);
   if (tid == 0) {
-    double ld = 0.0;
-    for (int q = 0; q < d; q++) ld += log(A[(size_t)q * d + q]);
-    ld *= 2.0;
+    const double ld = chol_logdet(A, d);
     logdet[j] = ld;
     const double lc = log(pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
     logc[j] = lc;
@@ -503,9 +450,7 @@ static int estep_plain_t(fem_em *h) {
     default: {
       nb = (n + 63) / 64;
       size_t sm = (size_t)64 * (d + 1) * sizeof(T);
-      if (sm > 48 * 1024)
-        FEM_CUDA(cudaFuncSetAttribute(k_estep_plain_generic<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      FEM_CUDA(allow_dyn_smem(k_estep_plain_generic<T>, sm));
       k_estep_plain_generic<T><<<(unsigned)nb, 64, sm, s>>>(h->X, n, d, K, mu, W, lc, R,
                                                             h->logl_part);
     }
@@ -542,9 +487,7 @@ static int launch_means(fem_em *h, int upt, int64_t rpb, size_t sm) {
   const T *R = (const T *)h->R;
 #define FEM_ML(U)                                                                          \
   if (upt == U) {                                                                          \
-    if (sm > 48 * 1024)                                                                    \
-      FEM_CUDA(cudaFuncSetAttribute(k_means_plain<T, C, U>,                                \
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)); \
+    FEM_CUDA(allow_dyn_smem(k_means_plain<T, C, U>, sm));                                  \
     k_means_plain<T, C, U><<<h->mgrid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, R,     \
                                                              h->mpart, rpb);               \
     return FEM_OK;                                                                         \
@@ -563,9 +506,7 @@ static int launch_cov(fem_em *h, int nb, int nblk, int64_t rpc, Src src, const T
   const int gx = (units + 255) / 256;
   const int cjmax = 256 / nblk + 2;
   size_t sm = (size_t)min(cjmax, h->k) * kCovTP * h->d * sizeof(T);
-  if (sm > 48 * 1024)
-    FEM_CUDA(cudaFuncSetAttribute(k_cov_plain<T, TB, Src>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sm));
+  FEM_CUDA(allow_dyn_smem(k_cov_plain<T, TB, Src>, sm));
   dim3 grid(gx, h->cchunks);
   k_cov_plain<T, TB, Src><<<grid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, src, mu, mu_ld, h->cpart, nb,
                                                         nblk, rpc);
@@ -604,15 +545,16 @@ template <typename T>
 static int mstep_plain_t(fem_em *h) {
   const int d = h->d, K = h->k;
   const int64_t n = h->n;
-  const int C = d < 32 ? d : 32;
-  const int units = K * (d / C);
+  // column chunk: the smallest of 4, 8, 16 covering d, else 32 (any d)
+  const int C = d <= 4 ? 4 : (d <= 8 ? 8 : (d <= 16 ? 16 : 32));
+  const int units = K * ((d + C - 1) / C);
   const int upt = units <= 256 ? 1 : (units <= 512 ? 2 : (units <= 1024 ? 4 : 0));
-  if (upt == 0 || d % C) {
+  if (upt == 0) {
     set_error("plain M-step: k*d too large (k=%d d=%d)", K, d);
     return FEM_ERR_UNSUPPORTED;
   }
   const int64_t rpb = (n + h->mgrid - 1) / h->mgrid;
-  size_t sm = (size_t)kMeanTP * d * sizeof(float) + (size_t)K * (kMeanTP + 1) * sizeof(T);
+  size_t sm = ((size_t)kMeanTP * d + C) * sizeof(float) + (size_t)K * (kMeanTP + 1) * sizeof(T);
   int st;
   switch (C) {
     case 4: st = launch_means<T, 4>(h, upt, rpb, sm); break;
@@ -637,13 +579,9 @@ int em_plain_mstep(fem_em *h) {
 
 constexpr size_t kJacobiSmem = 96 * 1024;
 
-// NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71): the
-// eigenvalues of each Sigma_j by cyclic Jacobi in FP64, one CTA per
-// component, on a copy in `work`.  Each sweep runs the n - 1 rounds of a
-// round-robin schedule; a round rotates n / 2 disjoint (p, q) pairs at once
-// (columns, then rows).  Sweeps stop when the off-diagonal mass is below
-// 1e-30 of the diagonal's, or after 100.  cond_j = |max eig / min eig|; the
-// largest over j is folded into *out (non-negative doubles order like their bits).
+// NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71), one
+// CTA per component on a symmetric copy of Sigma_j (block_jacobi_cond); the
+// largest cond_j is folded into *out (non-negative doubles order like their bits).
 __global__ void __launch_bounds__(256)
 k_cond_jacobi(const double *__restrict__ sigma, int d, double *__restrict__ work, unsigned long long *out) {
   extern __shared__ double smem_jac[];
@@ -651,86 +589,13 @@ k_cond_jacobi(const double *__restrict__ sigma, int d, double *__restrict__ work
   // the matrix lives in shared memory when it fits (d <= 110), else in `work`
   double *A = (size_t)d * d * sizeof(double) <= kJacobiSmem ? smem_jac : work + (size_t)j * d * d;
   const double *S = sigma + (size_t)j * d * d;
-  const int n = d + (d & 1);          // players of the round robin (a dummy when d is odd)
-  const int np = n / 2;
-  __shared__ double sc[128], ss[128];
-  __shared__ int sp[128], sq[128];
-  __shared__ double red_off[256], red_diag[256];
-  __shared__ int done;
   for (int e = tid; e < d * d; e += nt) {
     const int r = e / d, c = e - r * d;
     A[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
   }
   __syncthreads();
-  for (int sweep = 0; sweep < 100; sweep++) {
-    double off = 0.0, dg = 0.0;
-    for (int e = tid; e < d * d; e += nt) {
-      const int r = e / d, c = e - r * d;
-      const double v = A[e];
-      if (c > r) off += v * v;
-      else if (c == r) dg += v * v;
-    }
-    red_off[tid] = off;
-    red_diag[tid] = dg;
-    __syncthreads();
-    if (tid == 0) {
-      double o = 0.0, g = 0.0;
-      for (int t = 0; t < nt; t++) o += red_off[t], g += red_diag[t];
-      done = !(o > 1e-30 * g);
-    }
-    __syncthreads();
-    if (done) break;
-    for (int round = 0; round < n - 1; round++) {
-      for (int i = tid; i < np; i += nt) {
-        // position m holds player 0 (m = 0) or 1 + (m - 1 + round) mod (n - 1)
-        const int m1 = i, m2 = n - 1 - i;
-        const int p0 = m1 == 0 ? 0 : 1 + (m1 - 1 + round) % (n - 1);
-        const int q0 = 1 + (m2 - 1 + round) % (n - 1);
-        const int p = min(p0, q0), q = max(p0, q0);
-        double c = 1.0, s = 0.0;
-        if (q < d) {
-          const double apq = A[(size_t)p * d + q];
-          if (apq != 0.0) {
-            const double app = A[(size_t)p * d + p], aqq = A[(size_t)q * d + q];
-            const double th = (aqq - app) / (2.0 * apq);
-            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-            c = 1.0 / sqrt(t * t + 1.0);
-            s = t * c;
-          }
-        }
-        sc[i] = c, ss[i] = s, sp[i] = p, sq[i] = q;
-      }
-      __syncthreads();
-      for (int e = tid; e < d * np; e += nt) {     // columns p, q of every row
-        const int i = e / d, r = e - i * d;
-        const int p = sp[i], q = sq[i];
-        if (q < d && ss[i] != 0.0) {
-          const double arp = A[(size_t)r * d + p], arq = A[(size_t)r * d + q];
-          A[(size_t)r * d + p] = sc[i] * arp - ss[i] * arq;
-          A[(size_t)r * d + q] = ss[i] * arp + sc[i] * arq;
-        }
-      }
-      __syncthreads();
-      for (int e = tid; e < d * np; e += nt) {     // rows p, q of every column
-        const int i = e / d, r = e - i * d;
-        const int p = sp[i], q = sq[i];
-        if (q < d && ss[i] != 0.0) {
-          const double apr = A[(size_t)p * d + r], aqr = A[(size_t)q * d + r];
-          A[(size_t)p * d + r] = sc[i] * apr - ss[i] * aqr;
-          A[(size_t)q * d + r] = ss[i] * apr + sc[i] * aqr;
-        }
-      }
-      __syncthreads();
-    }
-  }
-  if (tid == 0) {
-    double mn = A[0], mx = A[0];
-    for (int p = 1; p < d; p++) {
-      mn = fmin(mn, A[(size_t)p * d + p]);
-      mx = fmax(mx, A[(size_t)p * d + p]);
-    }
-    atomicMax(out, (unsigned long long)__double_as_longlong(fabs(mx / mn)));
-  }
+  const double cond = block_jacobi_cond(A, d);
+  if (tid == 0) atomicMax(out, (unsigned long long)__double_as_longlong(cond));
 }
 
 int em_max_cond(fem_em *h, double *cond) {
@@ -742,7 +607,7 @@ int em_max_cond(fem_em *h, double *cond) {
   FEM_TRY(dalloc(&dout, 1));
   FEM_CUDA(cudaMemsetAsync(dout, 0, sizeof(unsigned long long), h->stream));
   const size_t sm = (size_t)h->d * h->d * sizeof(double) <= kJacobiSmem ? (size_t)h->d * h->d * sizeof(double) : 0;
-  if (sm > 48 * 1024) FEM_CUDA(cudaFuncSetAttribute(k_cond_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FEM_CUDA(allow_dyn_smem(k_cond_jacobi, sm));
   k_cond_jacobi<<<h->k, 256, sm, h->stream>>>(h->sigma, h->d, h->work, dout);
   cudaError_t e = cudaGetLastError();
   unsigned long long bits = 0;

@@ -16,6 +16,16 @@ namespace fem {
 // thread-local message of the last failing call (fem_last_error)
 void set_error(const char *fmt, ...);
 
+// Lets `func` launch with `bytes` of dynamic shared memory on the current
+// device.  The limit is a per-kernel attribute shared by every host thread, so
+// it is only ever raised (under a lock): a concurrent handle that needs less
+// never lowers it beneath another's launch of the same kernel.
+cudaError_t allow_dyn_smem(const void *func, size_t bytes);
+template <class F>
+cudaError_t allow_dyn_smem(F *func, size_t bytes) {
+  return allow_dyn_smem((const void *)func, bytes);
+}
+
 #define FEM_CUDA(call)                                                                  \
   do {                                                                                  \
     cudaError_t e_ = (call);                                                            \

@@ -263,8 +263,7 @@ int km_launch_assign_f32(fem_km *h) {
                     (size_t)256 * (D + 1) * 4;
 #define FEM_KA(DD)                                                                              \
   case DD:                                                                                      \
-    FEM_CUDA(cudaFuncSetAttribute(k_km_assign_f32<DD>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                  (int)sm));                                                    \
+    FEM_CUDA(allow_dyn_smem(k_km_assign_f32<DD>, sm));                                          \
     k_km_assign_f32<DD><<<h->grid, 256, sm, h->stream>>>(h->X, h->n, K, h->centf, h->cnorm,     \
                                                          h->cent, h->labels, h->acc, h->cnt,    \
                                                          ldexp(1.0, h->shift), h->dstat);       \

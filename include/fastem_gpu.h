@@ -143,6 +143,50 @@ int fem_em_timing_total(fem_em *h, double *train_ms, int64_t *sweeps);
  * rank-update part of EM2/MatrixEM.cpp:90-99) since the last reset */
 int fem_em_timing_covariance(fem_em *h, double *cov_ms);
 
+/* =========================== batched EM ============================== */
+
+/* Many independent fits trained together on one GPU.  No single reference
+ * counterpart: the reference trains one mixture per em2 run (EM2/main.cpp),
+ * and each fit here follows that run's loop, EMAlgorithm::TrainNoCopy
+ * (EM2/EMAlgorithm.cpp:139-191) with the SimpleMatrixEM sweep
+ * (EM2/MatrixEM.cpp:275-378), on its own data, with its own convergence test
+ * and failure status.  Every kernel of a sweep covers all fits still
+ * sweeping.  FP32 on CUDA cores with FP64 partial sums, factorisation and
+ * LogL: cfg->precision must be FEM_PREC_FP32 (cfg NULL: the reference
+ * defaults with FP32).  Per fit d <= 32, k <= 64, n < 2^31 (larger shapes:
+ * FEM_ERR_UNSUPPORTED). */
+typedef struct fem_em_batch fem_em_batch;
+
+int fem_em_batch_create(int nfits, const int *d, const int64_t *n, const int *k,
+                        const fem_em_config *cfg, fem_em_batch **out);
+void fem_em_batch_destroy(fem_em_batch *b);
+/* EMAlgorithm::SetParameters (EM2/EMAlgorithm.cpp:25-30), for every fit */
+int fem_em_batch_set_parameters(fem_em_batch *b, int max_sweeps, double eps, double abort_thr,
+                                double reg_coef);
+/* fit `fit`'s n x d float rows, ld floats apart (EM2/EMAlgorithm.cpp:225-235) */
+int fem_em_batch_upload(fem_em_batch *b, int fit, const float *X, int64_t ld);
+/* every fit's rows, packed one fit after another (fit 0's n0 x d0, then fit 1's ...) */
+int fem_em_batch_upload_packed(fem_em_batch *b, const float *X);
+/* EMAlgorithm::DecodeMixture (EM2/EMAlgorithm.cpp:125-131) for one fit */
+int fem_em_batch_set_params(fem_em_batch *b, int fit, const double *pi, const double *mu,
+                            const double *sigma);
+int fem_em_batch_get_params(fem_em_batch *b, int fit, double *pi, double *mu, double *sigma);
+/* trains every fit.  Per fit (arrays of nfits, each may be NULL): status is
+ * FEM_OK, FEM_ERR_CHOLESKY or FEM_ERR_COND_ABORT (what fem_em_train would
+ * return for that fit alone), iter_counter its IterCounter, logl its last
+ * LogL.  Returns FEM_OK when the batch ran, whatever the fits' statuses. */
+int fem_em_batch_train(fem_em_batch *b, int svd, int *status, int *iter_counter, double *logl);
+/* per-sweep LogL and e of one fit's last train (the first min(capacity,
+ * max_sweeps, 4096) sweeps) */
+int fem_em_batch_trace(fem_em_batch *b, int fit, double *logl_trace, double *e_trace, int capacity);
+/* the component whose Cholesky factorisation stopped the fit (-1: none) */
+int fem_em_batch_fail_component(fem_em_batch *b, int fit, int *component);
+/* per-phase device time (ms, CUDA events): [0] E-step, [1] means and their
+ * reduction, [2] covariance sums, [3] reduction + factorisation + sweep end,
+ * [4] the whole sweep loop; kernel launches and sweeps since enabling */
+int fem_em_batch_timing_enable(fem_em_batch *b, int on);
+int fem_em_batch_timing(fem_em_batch *b, double *phase_ms, int64_t *launches, int64_t *sweeps);
+
 /* ============================== k-means ============================== */
 
 typedef struct fem_km fem_km;

@@ -205,3 +205,51 @@ def test_illcond_d256_fp64_matches_oracle(gpu_lib, oracle):
     assert 1e5 < cond < 1e7
     with pytest.raises(Exception, match="mixed precision"):
         CudaMatrixEM(d, n, k, precision="mixed")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "mixed"])
+def test_concurrent_handles_of_different_shapes(gpu_lib, precision):
+    """Fits of different (d, K) from 8 host threads at once, one handle and
+    stream each, as a batched caller runs them: every fit succeeds and its
+    logL trace is identical to the same fit run alone.  The CUDA-core kernels
+    need per-shape dynamic shared memory (up to ~220 KB in FP64 at d = 32),
+    which concurrent handles must not lower beneath one another's launches."""
+    import concurrent.futures as cf
+    shapes = [(32, k) for k in (6, 9, 13, 18, 24, 30)] + [(16, k) for k in (8, 20, 31)] + [(8, 27)]
+    data = []
+    for i, (d, k) in enumerate(shapes):
+        X, _ = synth.kmeans_blobs(seed=100 + i, n=3000, d=d, k=k)
+        data.append((X, synth.dsquared_init(X, k, seed=i)))
+
+    def fit(i):
+        X, init = data[i]
+        with CudaMatrixEM(X.shape[1], len(X), len(init[0]), precision=precision) as em:
+            em.SetParameters(3, 0.0, 1e12)
+            em.Train(X, GaussianMixture(*init))
+            return em.logl_trace.copy()
+
+    with cf.ThreadPoolExecutor(8) as ex:
+        together = list(ex.map(fit, list(range(len(shapes))) * 3))
+    alone = [fit(i) for i in range(len(shapes))]
+    for j, tr in enumerate(together):
+        np.testing.assert_array_equal(tr, alone[j % len(shapes)])
+
+
+@pytest.mark.parametrize("d,precision", [(2, "fp64"), (5, "fp32"), (13, "fp64"), (37, "fp32"), (63, "fp64")])
+def test_plain_forms_any_dimension(gpu_lib, oracle, d, precision):
+    """The CUDA-core forms at dimensions that are not powers of two: ragged
+    column chunks in the means sums, 1- and 2-wide covariance tiles."""
+    X, _ = synth.kmeans_blobs(seed=900 + d, n=6000, d=d, k=5, spread=8.0)
+    init = synth.dsquared_init(X, 5, seed=d)
+    ref = oracle.em_train(X, *init, 4, eps=0.0, abort_thr=1e12)
+    assert ref["status"] == 0
+    got = run_gpu(X, init, 4, precision)
+    err = np.max(np.abs(got["logl"] - ref["logl"])) / len(X)
+    scale = np.max(np.abs(ref["mu"]))
+    if precision == "fp64":
+        assert err <= 1e-11
+        np.testing.assert_allclose(got["mu"], ref["mu"], rtol=1e-9, atol=1e-10 * scale)
+        np.testing.assert_allclose(got["sigma"], ref["sigma"], rtol=1e-8, atol=1e-10)
+    else:
+        assert err <= 1e-5
+        assert np.max(np.abs(got["mu"] - ref["mu"])) <= 1e-4 * scale
