@@ -63,6 +63,12 @@ __host__ __device__ constexpr int tri_off(int kk) {
 }
 __host__ __device__ constexpr int class_tb(int D) { return D >= 16 ? 8 : 4; }
 __host__ __device__ constexpr int class_nblk(int D) { return (D / class_tb(D)) * (D / class_tb(D) + 1) / 2; }
+// covariance sums: D <= 16 by component owners (k_b_cov_own), D = 32 by TB x TB blocks (k_b_cov)
+__host__ __device__ constexpr bool class_owner(int D) { return D <= 16; }
+__host__ __device__ constexpr int own_S(int D) { return D >= 16 ? 2 : 1; }          // threads per component
+__host__ __device__ constexpr int own_pairs(int D) { return D / 2 / own_S(D); }     // row pairs per thread
+__host__ __device__ constexpr int own_NE(int D) { return own_pairs(D) * (D + 1); }  // sums per thread
+__host__ __device__ constexpr int own_TP(int D) { return D >= 16 ? 32 : 128; }      // points per tile
 int class_of(int d) { return d <= 4 ? 0 : d <= 8 ? 1 : d <= 16 ? 2 : 3; }
 int class_dim(int c) { return 4 << c; }
 
@@ -127,6 +133,20 @@ __device__ __forceinline__ void blse_push(float l, float &mx, float &se) {
   }
 }
 
+// 4-byte asynchronous global -> shared copy; `valid` false writes zero
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+  const unsigned da = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(da), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+  const unsigned da = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(da), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // s_p += ||row KK of W . t_p||^2 for rows KK.. D-1 of a padded lower
 // triangle W, P centred points; rows by compile-time recursion so every
 // column bound is a constant, two interleaved accumulators per row for
@@ -182,7 +202,10 @@ constexpr int kBEPoints = kBEThreads * kBEP;     // points per item
 constexpr int kBEXs = kBEPoints + 1;             // transposed row stride (floats)
 
 template <int D>
-constexpr size_t estep_smem() { return (size_t)D * kBEXs * sizeof(float); }
+constexpr size_t estep_smem() {
+  constexpr int KC = D >= 32 ? 8 : 16;
+  return ((size_t)D * kBEXs + 2 * (size_t)((KC * tri_off(D) + KC * D + KC + 3) & ~3)) * sizeof(float);
+}
 
 template <int D, int P>
 __global__ void __launch_bounds__(kBEThreads)
@@ -191,10 +214,9 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
   static_assert(P == kBEP, "points per thread");
   constexpr int TRI = tri_off(D);
   constexpr int KC = D >= 32 ? 8 : 16;
-  extern __shared__ __align__(16) float sXt[];   // D x kBEXs
-  __shared__ __align__(16) float sW[KC * TRI];
-  __shared__ __align__(16) float smu[KC * D];
-  __shared__ float slc[KC];
+  constexpr int CB = KC * TRI + KC * D + KC;      // one component buffer: W, means, log coefficients
+  constexpr int CBP = (CB + 3) & ~3;
+  extern __shared__ __align__(16) float sXt[];   // D x kBEXs, then two component buffers
   __shared__ double red[kBEThreads / 32];
   const EItem item = items[blockIdx.x];
   if (!state[item.fit].active) return;
@@ -203,6 +225,17 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
   float *__restrict__ R = F.R;
   const int64_t n = F.n;
   const int d = F.d, K = F.k, tid = threadIdx.x;
+  float *cbuf = sXt + D * kBEXs;
+  // components [j0, j0 + kc) into buffer b (16-byte copies; W rows and means are 16-byte multiples)
+  auto stage = [&](int b, int j0) {
+    const int kc = min(KC, K - j0);
+    float *w = cbuf + b * CBP, *m = w + KC * TRI, *l = m + KC * D;
+    for (int e = tid; e < kc * TRI / 4; e += kBEThreads) cp_async16(w + 4 * e, F.WT + (size_t)j0 * TRI + 4 * e);
+    for (int e = tid; e < kc * D / 4; e += kBEThreads) cp_async16(m + 4 * e, F.muT + (size_t)j0 * D + 4 * e);
+    for (int e = tid; e < kc; e += kBEThreads) cp_async4(l + e, F.logcT + j0 + e, true);
+    cp_async_commit();
+  };
+  stage(0, 0);
   const int npts = (int)min((int64_t)kBEPoints, n - item.p0);
   // rows -> transposed columns (zero past the last point and past column d)
   if (d == D) {
@@ -233,17 +266,14 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
   float mx[P], se[P];
 #pragma unroll
   for (int p = 0; p < P; p++) mx[p] = -INFINITY, se[p] = 0.f;
-  for (int j0 = 0; j0 < K; j0 += KC) {
+  int b = 0;
+  for (int j0 = 0; j0 < K; j0 += KC, b ^= 1) {
     const int kc = min(KC, K - j0);
+    if (j0 + KC < K) stage(b ^ 1, j0 + KC);
+    else cp_async_commit();
+    cp_async_wait_prev();
     __syncthreads();
-    {
-      const float4 *src = reinterpret_cast<const float4 *>(F.WT + (size_t)j0 * TRI);
-      float4 *dst = reinterpret_cast<float4 *>(sW);
-      for (int e = tid; e < kc * TRI / 4; e += kBEThreads) dst[e] = src[e];
-      for (int e = tid; e < kc * D; e += kBEThreads) smu[e] = F.muT[(size_t)j0 * D + e];
-      if (tid < kc) slc[tid] = F.logcT[j0 + tid];
-    }
-    __syncthreads();
+    const float *sW = cbuf + b * CBP, *smu = sW + KC * TRI, *slc = smu + KC * D;
     for (int jj = 0; jj < kc; jj++) {
       const float *m = smu + jj * D;
       float t[P][D];
@@ -264,7 +294,9 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
         blse_push(l, mx[p], se[p]);
       }
     }
+    __syncthreads();
   }
+  cp_async_wait_all();
   double v = 0.0;
   float lse[P];
 #pragma unroll
@@ -272,6 +304,7 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
     lse[p] = mx[p] + logf(se[p]);
     if (valid[p]) v += (double)lse[p];
   }
+#pragma unroll 4
   for (int j = 0; j < K; j++) {
     float *Rj = R + (size_t)j * n;
 #pragma unroll
@@ -475,7 +508,7 @@ struct CovGeom {
 };
 
 template <int D>
-__global__ void __launch_bounds__(kBCThreads, 1)
+__global__ void __launch_bounds__(kBCThreads, 2)
 k_b_cov(const BFit *__restrict__ fits, const BState *__restrict__ state, const CItem *__restrict__ items,
         double *__restrict__ cpart) {
   using G = CovGeom<D>;
@@ -548,6 +581,7 @@ k_b_cov(const BFit *__restrict__ fits, const BState *__restrict__ state, const C
     }
     __syncthreads();
     if (t0 + TP < item.p1) fetch(t0 + TP);
+#pragma unroll 1
     for (int e = tid; e < CJ * TP * (D / 4); e += kBCThreads) {
       const int row = e / (D / 4), q4 = e - row * (D / 4);
       const int jj = row / TP, p = row - jj * TP;
@@ -563,31 +597,22 @@ k_b_cov(const BFit *__restrict__ fits, const BState *__restrict__ state, const C
     }
     __syncthreads();
     if (act) {
-      // two points per step (p, p + NG): both rows' loads are issued before the FMAs
       const float *zb = sZ + (size_t)cj * ZCS;
-      for (int p = g; p < TP; p += 2 * NG) {
-        const bool two = p + NG < TP;
-        float va[2][TB], vb[2][TB];
+#pragma unroll 1
+      for (int p = g; p < TP; p += NG) {
+        const float *zr = zb + p * ZP;
+        float va[TB], vb[TB];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          const float *zr = zb + (two ? p + h * NG : p) * ZP;
-#pragma unroll
-          for (int a4 = 0; a4 < TB / 4; a4++) {
-            const float4 u = *reinterpret_cast<const float4 *>(zr + bi * TB + 4 * a4);
-            const float4 v = *reinterpret_cast<const float4 *>(zr + bj * TB + 4 * a4);
-            va[h][4 * a4 + 0] = u.x, va[h][4 * a4 + 1] = u.y, va[h][4 * a4 + 2] = u.z, va[h][4 * a4 + 3] = u.w;
-            vb[h][4 * a4 + 0] = v.x, vb[h][4 * a4 + 1] = v.y, vb[h][4 * a4 + 2] = v.z, vb[h][4 * a4 + 3] = v.w;
-          }
+        for (int a4 = 0; a4 < TB / 4; a4++) {
+          const float4 u = *reinterpret_cast<const float4 *>(zr + bi * TB + 4 * a4);
+          const float4 v = *reinterpret_cast<const float4 *>(zr + bj * TB + 4 * a4);
+          va[4 * a4 + 0] = u.x, va[4 * a4 + 1] = u.y, va[4 * a4 + 2] = u.z, va[4 * a4 + 3] = u.w;
+          vb[4 * a4 + 0] = v.x, vb[4 * a4 + 1] = v.y, vb[4 * a4 + 2] = v.z, vb[4 * a4 + 3] = v.w;
         }
-        if (!two)
 #pragma unroll
-          for (int a = 0; a < TB; a++) va[1][a] = 0.f;
+        for (int a = 0; a < TB; a++)
 #pragma unroll
-        for (int h = 0; h < 2; h++)
-#pragma unroll
-          for (int a = 0; a < TB; a++)
-#pragma unroll
-            for (int b = 0; b < TB; b++) acc[a][b] = fmaf(va[h][a], vb[h][b], acc[a][b]);
+          for (int b = 0; b < TB; b++) acc[a][b] = fmaf(va[a], vb[b], acc[a][b]);
       }
     }
   }
@@ -600,13 +625,133 @@ k_b_cov(const BFit *__restrict__ fits, const BState *__restrict__ state, const C
   }
 }
 
-// partial-block geometry of one covariance unit range (shared by host and device)
-__host__ __device__ inline void unit_range(int k, int D, int ug, int *u0, int *u1, int *ng) {
+// Partial geometry of covariance unit range `ug` of a fit with k components
+// in class D: units [u0, u1), ng point groups, per doubles per unit; the
+// range's partials are ng x (u1 - u0) x per doubles.  Block layout (D = 32):
+// a unit is one TB x TB block of one component, ranges of <= 256 units.
+// Owner layout (D <= 16): one range whose units are the k components, each
+// owned by own_S(D) threads of own_NE(D) sums.
+__host__ __device__ inline void unit_range(int k, int D, int ug, int *u0, int *u1, int *ng, int *per) {
+  if (class_owner(D)) {
+    *u0 = 0;
+    *u1 = k;
+    *ng = 256 / (own_S(D) * ((k + 31) & ~31));
+    *per = own_S(D) * own_NE(D);
+    return;
+  }
   const int total = k * class_nblk(D);
   *u0 = ug * 256;
   *u1 = min(total, *u0 + 256);
   const int UG = (*u1 - *u0 + 31) & ~31;
   *ng = 256 / UG;
+  *per = class_tb(D) * class_tb(D);
+}
+
+// one point's contribution r u u^T to the sums of row pairs I.. of the
+// thread set SS: pair q covers rows q (columns q..D-1) and D-1-q (columns
+// D-1-q..D-1), D + 1 sums; compile-time recursion keeps every index constant
+template <int D, int SS, int I>
+__device__ __forceinline__ void own_pairs_acc(const float (&u)[D], float r, float (&acc)[own_NE(D)]) {
+  constexpr int S = own_S(D), q = SS + S * I, q2 = D - 1 - q, base = I * (D + 1);
+  const float ra = r * u[q], rb = r * u[q2];
+#pragma unroll
+  for (int c = q; c < D; c++) acc[base + c - q] = fmaf(ra, u[c], acc[base + c - q]);
+#pragma unroll
+  for (int c = q2; c < D; c++) acc[base + (D - q) + c - q2] = fmaf(rb, u[c], acc[base + (D - q) + c - q2]);
+  if constexpr (I + 1 < own_pairs(D)) own_pairs_acc<D, SS, I + 1>(u, r, acc);
+}
+
+// shared memory of k_b_cov_own<D> for classes with at most kmax components:
+// two buffers of (TP x D rows, kmax x (TP + 1) posteriors); the odd row
+// stride keeps the lanes of a warp (consecutive components, one point) in
+// different banks
+__host__ __device__ constexpr size_t own_buf_floats(int D, int kmax) {
+  return ((size_t)own_TP(D) * D + (size_t)kmax * (own_TP(D) + 1) + 3) & ~(size_t)3;
+}
+
+// MatrixEMBase::ComputeWeightedTempDataset + BlockCovariances
+// (EM2/MatrixEM.cpp:53-67,90-99) for D <= 16: CovSum_j += r_ij u u^T with
+// u = x_i - mu_j formed on the fly from a staged tile of rows.  A component
+// is owned by own_S(D) threads (a warp-uniform split of its row pairs), the
+// CTA's 256 / (own_S roundup32(k)) point groups split each tile's points.
+// Tiles are copied asynchronously one tile ahead into two shared buffers.
+// FP32 sums over the item; partials [group][thread set][component][own_NE]
+// in FP64.
+template <int D>
+__global__ void __launch_bounds__(kBCThreads, D >= 16 ? 1 : 2)
+k_b_cov_own(const BFit *__restrict__ fits, const BState *__restrict__ state, const CItem *__restrict__ items,
+            double *__restrict__ cpart, int kmax) {
+  constexpr int S = own_S(D), NE = own_NE(D), TP = own_TP(D);
+  extern __shared__ __align__(16) float osm[];
+  const CItem item = items[blockIdx.x];
+  if (!state[item.fit].active) return;
+  const BFit &F = fits[item.fit];
+  const float *__restrict__ X = F.X;
+  const float *__restrict__ R = F.R;
+  const int64_t n = F.n;
+  const int d = F.d, K = F.k, tid = threadIdx.x;
+  const int KG = (K + 31) & ~31, UG = S * KG, NG = kBCThreads / UG;
+  const int ul = tid % UG, g = tid / UG, ts = ul / KG, j = ul - ts * KG;
+  const bool act = j < K && g < NG;
+  const size_t bufsz = own_buf_floats(D, kmax);
+  float mu[D];
+#pragma unroll
+  for (int q = 0; q < D; q++) mu[q] = act ? F.muT[(size_t)j * D + q] : 0.f;
+  float acc[NE];
+#pragma unroll
+  for (int e = 0; e < NE; e++) acc[e] = 0.f;
+  // one tile of rows (TP x D, zero past d and past the item) and posteriors (K x TP)
+  auto stage = [&](int buf, int t0) {
+    float *sx = osm + buf * bufsz, *sr = sx + TP * D;
+    const int tp = min(TP, item.p1 - t0);
+    for (int e = tid; e < TP * D; e += kBCThreads) {
+      const int p = e / D, q = e - p * D;
+      const bool v = p < tp && q < d;
+      cp_async4(sx + e, X + (v ? (size_t)(t0 + p) * d + q : 0), v);
+    }
+    for (int e = tid; e < K * TP; e += kBCThreads) {
+      const int jj = e / TP, p = e - jj * TP;
+      const bool v = p < tp;
+      cp_async4(sr + jj * (TP + 1) + p, R + (size_t)jj * n + (v ? t0 + p : 0), v);
+    }
+    cp_async_commit();
+  };
+  stage(0, item.p0);
+  int buf = 0;
+  for (int t0 = item.p0; t0 < item.p1; t0 += TP, buf ^= 1) {
+    if (t0 + TP < item.p1) stage(buf ^ 1, t0 + TP);
+    else cp_async_commit();                 // an empty group keeps the wait count uniform
+    cp_async_wait_prev();
+    __syncthreads();
+    const float *sx = osm + buf * bufsz, *sr = sx + TP * D;
+    const int tp = min(TP, item.p1 - t0);
+    if (act) {
+      for (int p = g; p < tp; p += NG) {
+        const float r = sr[j * (TP + 1) + p];
+        float u[D];
+#pragma unroll
+        for (int q4 = 0; q4 < D / 4; q4++) {
+          const float4 xv = *reinterpret_cast<const float4 *>(sx + p * D + 4 * q4);
+          u[4 * q4 + 0] = xv.x - mu[4 * q4 + 0];
+          u[4 * q4 + 1] = xv.y - mu[4 * q4 + 1];
+          u[4 * q4 + 2] = xv.z - mu[4 * q4 + 2];
+          u[4 * q4 + 3] = xv.w - mu[4 * q4 + 3];
+        }
+        if constexpr (S == 1) {
+          own_pairs_acc<D, 0, 0>(u, r, acc);
+        } else {
+          if (ts == 0) own_pairs_acc<D, 0, 0>(u, r, acc);
+          else own_pairs_acc<D, 1, 0>(u, r, acc);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (act) {
+    double *o = cpart + item.part + ((size_t)(g * S + ts) * K + j) * NE;
+#pragma unroll
+    for (int e = 0; e < NE; e++) o[e] = (double)acc[e];
+  }
 }
 
 // ======================================================= factorisation
@@ -628,35 +773,57 @@ k_b_factor(const BFit *__restrict__ fits, BState *__restrict__ state, const int2
   const int d = F.d, D = F.D, K = F.k;
   double *S = F.sigma + (size_t)j * d * d;
   if (reduce) {
-    const int TB = class_tb(D), NB = D / TB, NBLK = class_nblk(D), per = TB * TB;
     const double inv = 1.0 / F.psum[j];
-    for (int e = tid; e < NBLK * per; e += kBFThreads) {
-      const int b = e / per, w = e - b * per;
-      int bi = 0, bb = b;
-      while (bb >= NB - bi) {
-        bb -= NB - bi;
-        bi++;
+    if (class_owner(D)) {
+      const int Sd = own_S(D), NE = own_NE(D);
+      int u0 = 0, u1 = 0, ng = 0, per = 0;
+      unit_range(K, D, 0, &u0, &u1, &ng, &per);
+      for (int e = tid; e < d * d; e += kBFThreads) {
+        const int a = e / d, c = e - a * d;
+        if (a > c) continue;
+        const bool first = a < D / 2;
+        const int q = first ? a : D - 1 - a;
+        const int ts = q % Sd, i = q / Sd;
+        const int w = i * (D + 1) + (first ? c - a : (D - q) + (c - a));
+        double s2 = 0.0;
+        for (int ch = 0; ch < F.c_chunks; ch++) {
+          const double *pp = cpart + F.c_part + ch * F.c_stride + ((size_t)ts * K + j) * NE + w;
+          for (int gg = 0; gg < ng; gg++) s2 += pp[(size_t)gg * Sd * K * NE];
+        }
+        s2 *= inv;
+        S[(size_t)a * d + c] = s2;
+        S[(size_t)c * d + a] = s2;
       }
-      const int bj = bi + bb;
-      const int a = bi * TB + w / TB, c = bj * TB + (w % TB);
-      if (a > c || c >= d) continue;
-      const int unit = j * NBLK + b, ug = unit / 256, ul = unit - ug * 256;
-      int64_t off = 0;
-      int u0 = 0, u1 = 0, ng = 0;
-      for (int q = 0; q < ug; q++) {
-        unit_range(K, D, q, &u0, &u1, &ng);
-        off += (int64_t)ng * (u1 - u0) * per;
+    } else {
+      const int TB = class_tb(D), NB = D / TB, NBLK = class_nblk(D), per = TB * TB;
+      for (int e = tid; e < NBLK * per; e += kBFThreads) {
+        const int b = e / per, w = e - b * per;
+        int bi = 0, bb = b;
+        while (bb >= NB - bi) {
+          bb -= NB - bi;
+          bi++;
+        }
+        const int bj = bi + bb;
+        const int a = bi * TB + w / TB, c = bj * TB + (w % TB);
+        if (a > c || c >= d) continue;
+        const int unit = j * NBLK + b, ug = unit / 256, ul = unit - ug * 256;
+        int64_t off = 0;
+        int u0 = 0, u1 = 0, ng = 0, pr = 0;
+        for (int q = 0; q < ug; q++) {
+          unit_range(K, D, q, &u0, &u1, &ng, &pr);
+          off += (int64_t)ng * (u1 - u0) * pr;
+        }
+        unit_range(K, D, ug, &u0, &u1, &ng, &pr);
+        const int nu = u1 - u0;
+        double s2 = 0.0;
+        for (int ch = 0; ch < F.c_chunks; ch++) {
+          const double *pp = cpart + F.c_part + ch * F.c_stride + off + (size_t)ul * per + w;
+          for (int gg = 0; gg < ng; gg++) s2 += pp[(size_t)gg * nu * per];
+        }
+        s2 *= inv;
+        S[(size_t)a * d + c] = s2;
+        S[(size_t)c * d + a] = s2;
       }
-      unit_range(K, D, ug, &u0, &u1, &ng);
-      const int nu = u1 - u0;
-      double s = 0.0;
-      for (int ch = 0; ch < F.c_chunks; ch++) {
-        const double *pp = cpart + F.c_part + ch * F.c_stride + off + (size_t)ul * per + w;
-        for (int gg = 0; gg < ng; gg++) s += pp[(size_t)gg * nu * per];
-      }
-      s *= inv;
-      S[(size_t)a * d + c] = s;
-      S[(size_t)c * d + a] = s;
     }
     __syncthreads();
   }
@@ -771,6 +938,7 @@ struct fem_em_batch {
   int ncomps = 0;
   int e_beg[kClasses + 1] = {}, m_beg[kClasses + 1] = {}, c_beg[kClasses + 1] = {};
   size_t c_smem[kClasses] = {};
+  int c_kmax[kClasses] = {};       // largest k of the class's fits
   std::vector<BState> hstate;
   // timing: phase boundaries of the sweeps since the last host sync
   bool timing = false;
@@ -893,9 +1061,9 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     const CItem *it0 = b->citems + b->c_beg[c];
     const size_t sm = b->c_smem[c];
     switch (c) {
-      case 0: k_b_cov<4><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
-      case 1: k_b_cov<8><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
-      case 2: k_b_cov<16><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
+      case 0: k_b_cov_own<4><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart, b->c_kmax[c]); break;
+      case 1: k_b_cov_own<8><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart, b->c_kmax[c]); break;
+      case 2: k_b_cov_own<16><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart, b->c_kmax[c]); break;
       default: k_b_cov<32><<<cnt, kBCThreads, sm, b->stream>>>(fits, st, it0, b->cpart); break;
     }
     FEM_CUDA(cudaGetLastError());
@@ -1031,21 +1199,20 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
         mp += (int64_t)F.k * (F.D + 4);
       }
       F.m_count = (int)mi.size() - F.m_first;
-      const int per = class_tb(F.D) * class_tb(F.D);
-      F.nug = (F.k * class_nblk(F.D) + 255) / 256;
+      F.nug = class_owner(F.D) ? 1 : (F.k * class_nblk(F.D) + 255) / 256;
       F.c_part = cp;
       F.c_stride = 0;
       for (int ug = 0; ug < F.nug; ug++) {
-        int u0, u1, ng;
-        unit_range(F.k, F.D, ug, &u0, &u1, &ng);
+        int u0, u1, ng, per;
+        unit_range(F.k, F.D, ug, &u0, &u1, &ng, &per);
         F.c_stride += (int64_t)ng * (u1 - u0) * per;
       }
       F.c_chunks = 0;
       for (int64_t p = 0; p < F.n; p += kBCChunk) {
         int64_t off = cp;
         for (int ug = 0; ug < F.nug; ug++) {
-          int u0, u1, ng;
-          unit_range(F.k, F.D, ug, &u0, &u1, &ng);
+          int u0, u1, ng, per;
+          unit_range(F.k, F.D, ug, &u0, &u1, &ng, &per);
           ci.push_back(CItem{f, (int)p, (int)std::min<int64_t>(F.n, p + kBCChunk), u0, u1, off});
           off += (int64_t)ng * (u1 - u0) * per;
         }
@@ -1055,14 +1222,8 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
     }
     const int D = class_dim(c), nblk = class_nblk(D);
     const int cj = std::max(1, std::min(kmax, 256 / nblk + 2));
-    size_t fl = 0;
-    switch (c) {
-      case 0: fl = CovGeom<4>::floats(cj); break;
-      case 1: fl = CovGeom<8>::floats(cj); break;
-      case 2: fl = CovGeom<16>::floats(cj); break;
-      default: fl = CovGeom<32>::floats(cj); break;
-    }
-    b->c_smem[c] = fl * sizeof(float);
+    b->c_kmax[c] = std::max(kmax, 1);
+    b->c_smem[c] = (class_owner(D) ? 2 * own_buf_floats(D, b->c_kmax[c]) : CovGeom<32>::floats(cj)) * sizeof(float);
   }
   b->e_beg[kClasses] = (int)ei.size();
   b->m_beg[kClasses] = (int)mi.size();
@@ -1088,11 +1249,13 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
     set_error("event creation failed");
     return fail(FEM_ERR_CUDA);
   }
-  if (allow_dyn_smem(k_b_estep<16, kBEP>, estep_smem<16>()) != cudaSuccess ||
+  if (allow_dyn_smem(k_b_estep<4, kBEP>, estep_smem<4>()) != cudaSuccess ||
+      allow_dyn_smem(k_b_estep<8, kBEP>, estep_smem<8>()) != cudaSuccess ||
+      allow_dyn_smem(k_b_estep<16, kBEP>, estep_smem<16>()) != cudaSuccess ||
       allow_dyn_smem(k_b_estep<32, kBEP>, estep_smem<32>()) != cudaSuccess ||
-      allow_dyn_smem(k_b_cov<4>, b->c_smem[0]) != cudaSuccess ||
-      allow_dyn_smem(k_b_cov<8>, b->c_smem[1]) != cudaSuccess ||
-      allow_dyn_smem(k_b_cov<16>, b->c_smem[2]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov_own<4>, b->c_smem[0]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov_own<8>, b->c_smem[1]) != cudaSuccess ||
+      allow_dyn_smem(k_b_cov_own<16>, b->c_smem[2]) != cudaSuccess ||
       allow_dyn_smem(k_b_cov<32>, b->c_smem[3]) != cudaSuccess) {
     set_error("batched kernels' shared-memory limits could not be raised");
     return fail(FEM_ERR_CUDA);

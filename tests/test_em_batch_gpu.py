@@ -104,7 +104,11 @@ def test_batch_failures_stop_only_their_fit(gpu_lib, oracle):
     got = train_batch(data, 8)
     ref = oracle.em_train(collapse[0], *collapse[1], 8, eps=0.0, abort_thr=1e12)
     assert ref["status"] == C.FEM_ERR_CHOLESKY
-    assert got["status"][3] == C.FEM_ERR_CHOLESKY and got["iters"][3] == ref["iter_counter"]
+    # the sweep in which a collapsing covariance stops being positive definite
+    # depends on rounding: FP32 sums may cross it one sweep apart from FP64
+    assert got["status"][3] == C.FEM_ERR_CHOLESKY and abs(got["iters"][3] - ref["iter_counter"]) <= 1
+    m = min(len(got["traces"][3][0]), len(ref["logl"]))
+    assert np.max(np.abs(got["traces"][3][0][:m] - ref["logl"][:m])) / len(collapse[0]) <= 1e-5
     assert got["status"][4] == C.FEM_ERR_CHOLESKY and got["iters"][4] == 0 and got["fail"][4] == 0
     alone = train_batch(good, 8)
     for i in range(3):
