@@ -123,8 +123,8 @@ struct TcEmPlan {
   int64_t np = 0;                       // padded row pitch (multiple of 64)
   float *lsc = nullptr;                 // E-step scratch: egrid x 2 x K x 256
   double *epart = nullptr;              // per-CTA log-likelihood
-  double *mpart = nullptr;              // means partials: mgrid x 128 x 80
-  double *cpart = nullptr;              // covariance partials: cgrid x 4 x 64 x 64
+  double *mpart = nullptr;              // means partials: mgrid x 80 columns x 128 components
+  double *cpart = nullptr;              // covariance partials: cgrid x 2 pairs x 64 columns x 128 rows
   double *dpart = nullptr;              // exact diagonals: cgrid x 4 x 64
   float *muf = nullptr;                 // new means (float) for the covariance producers
   float *chi = nullptr;                 // float(log coefficient); -inf for padding components
@@ -478,11 +478,13 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
       mbar_wait_drain(&S.mma_done, 0);
     }
   } else {
-    // flush: lane row = component; 80 columns -> FP64 partial
+    // flush: lane row = component; 80 columns -> this CTA's FP64 partial,
+    // column-major (column c of component comp at o[c * kMaxK]) so a warp's
+    // 32 components are 256 contiguous bytes
     const int quad = warp & 3;
     const int comp = quad * 32 + lane;
-    double *o = part + ((size_t)blockIdx.x * kMaxK + comp) * kMeanN;   // this CTA's FP64 partial
-    for (int c = 0; c < kMeanN; c++) o[c] = 0.0;
+    double *o = part + (size_t)blockIdx.x * kMaxK * kMeanN + comp;
+    for (int c = 0; c < kMeanN; c++) o[(size_t)c * kMaxK] = 0.0;
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
       const int ab = w & 1;
@@ -496,7 +498,7 @@ k_means_tc(const __grid_constant__ CUtensorMap tm_rh, const __grid_constant__ CU
         tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 32; c++)
-          if (c0 + c < kMeanN) o[c0 + c] += (double)__uint_as_float(v[c]);
+          if (c0 + c < kMeanN) o[(size_t)(c0 + c) * kMaxK] += (double)__uint_as_float(v[c]);
       }
       tc_fence_before();
       __syncwarp();
@@ -517,7 +519,7 @@ __global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, 
   __shared__ double s1;
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int g = 0; g < G; g++) s += part[((size_t)g * kMaxK + j) * kMeanN + kD];
+    for (int g = 0; g < G; g++) s += part[((size_t)g * kMeanN + kD) * kMaxK + j];
     s1 = s;
     psum[j] = s;
     pi[j] = s / (double)n;
@@ -525,7 +527,7 @@ __global__ void k_final_means_tc(const double *__restrict__ part, int G, int K, 
   __syncthreads();
   for (int q = threadIdx.x; q < kD; q += blockDim.x) {
     double s = 0.0;
-    for (int g = 0; g < G; g++) s += part[((size_t)g * kMaxK + j) * kMeanN + q];
+    for (int g = 0; g < G; g++) s += part[((size_t)g * kMeanN + q) * kMaxK + j];
     const double m = s / s1;
     if (q < d) mu[(size_t)j * d + q] = m;
     muf[(size_t)j * kD + q] = q < d ? (float)m : 0.f;
@@ -720,11 +722,13 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
     const int quad = warp & 3;
     const int lrow = quad * 32 + lane;          // TMEM lane = row of the pair tile
     const int half = lrow >> 6;                 // 0: first component of the pair, 1: second
-    double *o[2];                               // this CTA's FP64 partial rows
+    // this CTA's FP64 partials, column-major per pair: column c of pair pr at
+    // o[pr][c * 128] (row lrow), so a warp's 32 rows are 256 contiguous bytes
+    double *o[2];
 #pragma unroll
     for (int pr = 0; pr < 2; pr++) {
-      o[pr] = cpart + ((cta * 4 + pr * 2 + half) * kD + (lrow & 63)) * kD;
-      for (int c = 0; c < kD; c++) o[pr][c] = 0.0;
+      o[pr] = cpart + (cta * 2 + pr) * (size_t)(kD * 128) + lrow;
+      for (int c = 0; c < kD; c++) o[pr][(size_t)c * 128] = 0.0;
     }
     bool ok = true;
     for (int64_t w = 0; w < nwin && ok; w++) {
@@ -739,7 +743,7 @@ k_cov_tc(const __grid_constant__ CUtensorMap tm_x32, const __grid_constant__ CUt
           tmem_ld32(tbase + ((uint32_t)(quad * 32) << 16) + ab * 256 + pr * 128 + half * 64 + c0, v);
           tmem_wait_ld();
 #pragma unroll
-          for (int c = 0; c < 32; c++) o[pr][c0 + c] += (double)__uint_as_float(v[c]);
+          for (int c = 0; c < 32; c++) o[pr][(size_t)(c0 + c) * 128] += (double)__uint_as_float(v[c]);
         }
       }
       tc_fence_before();
@@ -766,9 +770,10 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
     if (a == b) {
       for (int c = 0; c < gy; c++) s += dpart[(((size_t)c * gx + grp) * 4 + q) * kD + a];
     } else {
+      // partials of CTA (chunk c, group grp): pair q / 2, rows (q % 2) * 64 + row, column-major
       for (int c = 0; c < gy; c++) {
-        const double *P = cpart + (((size_t)c * gx + grp) * 4 + q) * kD * kD;
-        s += 0.5 * (P[a * kD + b] + P[b * kD + a]);
+        const double *P = cpart + (((size_t)c * gx + grp) * 2 + (q >> 1)) * (kD * 128) + (q & 1) * 64;
+        s += 0.5 * (P[(size_t)b * 128 + a] + P[(size_t)a * 128 + b]);
       }
     }
     s *= inv;
