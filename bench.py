@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--workload", default="em", choices=["em", "kmeans", "batched"])
     ap.add_argument("--n", type=int, default=None, help="points (default 2^23 EM, 2^24 k-means)")
     ap.add_argument("--k", type=int, default=128)
+    ap.add_argument("--fits-d", type=int, default=None, choices=[4, 8, 16, 32],
+                    help="batched workload: only the fits of this dimension (a smaller case for profiling)")
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core comparison")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -359,6 +361,7 @@ def main():
 
 BATCH_METRIC = "batched EM fits/s: 512 fits, N in [2e3,2e5], d in {4,8,16,32}, K in [2,32], 30 sweeps"
 BATCH_SWEEPS = 30
+BATCH_PROFILE_FILE = os.path.join(ROOT, "profiles", "batch_em_512fits.md")
 
 
 def batched_workload():
@@ -396,6 +399,9 @@ def run_batched(args, rank, world, local):
     |dlogL/N| against the FP64 oracle is reported for a sample of fits.
     With --gpus N each rank trains its own copy of the batch (replicas)."""
     fits, data = batched_workload()
+    if args.fits_d:
+        keep = [i for i, f in enumerate(fits) if f["d"] == args.fits_d]
+        fits, data = [fits[i] for i in keep], [data[i] for i in keep]
     nf = len(fits)
     if args.impl == "reference":
         if rank == 0:
@@ -500,29 +506,40 @@ def run_batched(args, rank, world, local):
     dist.close()
     if rank != 0:
         return
-    # roofline: the covariance sums (the largest phase), FP32 CUDA-core flops
-    # N K d (d + 1) per fit and sweep against the nominal FP32 rate at the
-    # sampled SM clock (152 SMs x 128 lanes x 2 flop)
-    cov_flop = sum(n * k * d * (d + 1) for d, n, k in shapes) * BATCH_SWEEPS
-    cov_s = tm["cov_ms"] / 1e3 / args.steps
+    # roofline: the largest kernel, the covariance sums of the d = 32 class
+    # (k_b_cov<32>), FP32 CUDA-core flops N K d (d + 1) per fit and sweep against
+    # the nominal FP32 rate at the sampled SM clock (152 SMs x 128 lanes x 2 flop);
+    # traffic per launch from the committed ncu summary
+    cov_flop = sum(n * k * d * (d + 1) for d, n, k in shapes if d > 16) * BATCH_SWEEPS
+    cov_s = tm["classes"][32]["cov_ms"] / 1e3 / args.steps
     mhz = clk.get("sm_mhz") or 2070.0
     peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-    achieved = cov_flop / cov_s / 1e12
+    achieved = cov_flop / cov_s / 1e12 if cov_s > 0 else None
+    traffic = None
+    try:
+        for ln in open(BATCH_PROFILE_FILE):
+            if ln.startswith("traffic_bytes_per_launch k_b_cov<32>"):
+                traffic = float(ln.split("=")[-1])
+    except OSError:
+        pass
     per_step = {k2: tm[k2] / args.steps for k2 in ("estep_ms", "means_ms", "cov_ms", "factor_ms", "loop_ms")}
+    per_class = {"d<=%d" % D: {k2: v / args.steps for k2, v in tm["classes"][D].items()} for D in (4, 8, 16, 32)}
     line = {
         "metric": BATCH_METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 (CUDA cores), fp64 sums / factorisation / logL",
         "data": "synthetic blobs per fit seed (synth.em_batched, seed 4)",
-        "config": {"workload": "512 fits x 30 sweeps per step, batched engine (every kernel covers all fits)",
+        "config": {"workload": ("%d fits x 30 sweeps per step, batched engine (every kernel covers all fits)" % nf)
+                   + (", only the d = %d fits" % args.fits_d if args.fits_d else ""),
                    "total_points": int(sum(f["n"] for f in fits)), "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (rows %.2f GB, posteriors %.2f GB)" % (
                        x_bytes / 1e9, sum(n * k for d, n, k in shapes) * 4 / 1e9)},
-        "phase_ms_per_step": per_step,
-        "roofline": {"kernel": "k_b_cov (all dimension classes)", "bound": "fp32", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+        "phase_ms_per_step": per_step, "class_ms_per_step": per_class,
+        "roofline": {"kernel": "k_b_cov<32> (covariance sums, d = 32 fits)", "bound": "fp32", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": "nominal FP32 CUDA-core rate at the sampled SM clock (no measured FP32 peak)",
-                     "traffic": None, "algorithmic_flop_per_step": cov_flop},
+                     "traffic": traffic, "algorithmic_flop_per_step": cov_flop,
+                     "launch_ms": cov_s * 1e3 / BATCH_SWEEPS},
         "failed_fits": int((st != 0).sum()), "failed_fits_oracle_agrees": "fits 282, 283, 385 collapse in FP64",
         "max_dlogL_per_N_sampled": max(errs) if errs else None, "sampled_fits": len(errs),
         "per_fit_handles": per_fit, "speedup_vs_per_fit_handles": (value / per_fit["value"]) if per_fit else None,

@@ -37,6 +37,7 @@ EXPORTS = [
     "fem_em_batch_upload", "fem_em_batch_upload_packed", "fem_em_batch_set_params",
     "fem_em_batch_get_params", "fem_em_batch_train", "fem_em_batch_trace",
     "fem_em_batch_fail_component", "fem_em_batch_timing_enable", "fem_em_batch_timing",
+    "fem_em_batch_timing_classes",
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
@@ -119,6 +120,7 @@ def lib():
         "fem_em_batch_fail_component": ([P, i32, P], i32),
         "fem_em_batch_timing_enable": ([P, i32], i32),
         "fem_em_batch_timing": ([P, P, P, P], i32),
+        "fem_em_batch_timing_classes": ([P, P], i32),
         "fem_km_config_default": ([ctypes.POINTER(KmConfig)], None),
         "fem_km_create": ([i32, i64, i32, ctypes.POINTER(KmConfig), pP], i32),
         "fem_km_destroy": ([P], None),

@@ -118,5 +118,8 @@ class CudaBatchEM:
         ms = np.zeros(5)
         launches, sweeps = ctypes.c_int64(0), ctypes.c_int64(0)
         C.check(C.lib().fem_em_batch_timing(self._h, C.ptr(ms), ctypes.byref(launches), ctypes.byref(sweeps)))
+        cls = np.zeros(12)
+        C.check(C.lib().fem_em_batch_timing_classes(self._h, C.ptr(cls)))
+        per = {D: dict(estep_ms=cls[c], means_ms=cls[4 + c], cov_ms=cls[8 + c]) for c, D in enumerate((4, 8, 16, 32))}
         return dict(estep_ms=ms[0], means_ms=ms[1], cov_ms=ms[2], factor_ms=ms[3], loop_ms=ms[4],
-                    launches=launches.value, sweeps=sweeps.value)
+                    launches=launches.value, sweeps=sweeps.value, classes=per)

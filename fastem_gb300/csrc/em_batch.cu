@@ -52,6 +52,7 @@ constexpr int kBCChunk = 4096;   // points per covariance item
 constexpr int kBMTile = 32;      // points staged per means tile
 constexpr int kBCTile = 16;      // points staged per covariance tile
 constexpr int kBatchSyncEvery = 8;
+constexpr int kTimeMarks = 15;   // timing events per sweep (see collect_timing)
 constexpr int kClasses = 4;      // D = 4, 8, 16, 32
 
 // padded lower triangle: row kk holds kk + 1 entries in 4 * ceil((kk + 1) / 4) floats
@@ -942,9 +943,10 @@ struct fem_em_batch {
   std::vector<BState> hstate;
   // timing: phase boundaries of the sweeps since the last host sync
   bool timing = false;
-  cudaEvent_t pev[kBatchSyncEvery][5] = {};
+  cudaEvent_t pev[kBatchSyncEvery][kTimeMarks] = {};
   cudaEvent_t ev_start = nullptr, ev_end = nullptr;
   double t_phase[5] = {};           // E-step, means, covariance, factorisation, whole sweep loop
+  double t_class[3][kClasses] = {}; // E-step, means, covariance launches per dimension class
   int64_t launches = 0, sweeps = 0;
 };
 
@@ -1007,16 +1009,26 @@ int upload_vec(T **dst, const std::vector<T> &v) {
 }
 
 
-void mark(fem_em_batch *b, int slot, int phase) {
-  if (b->timing) cudaEventRecord(b->pev[slot][phase], b->stream);
+void mark(fem_em_batch *b, int slot, int m) {
+  if (b->timing) cudaEventRecord(b->pev[slot][m], b->stream);
 }
 
-// per-phase device time of the sweeps recorded in event slots [0, pending)
+// device time of the sweeps recorded in event slots [0, pending); marks: 0 sweep
+// start, 1..4 after each class's E-step, 5..8 after each class's means, 9 after
+// their reduction, 10..13 after each class's covariance sums, 14 sweep end
 void collect_timing(fem_em_batch *b, int pending) {
   float ms = 0.f;
-  for (int s = 0; s < pending; s++)
+  for (int s = 0; s < pending; s++) {
+    const cudaEvent_t *e = b->pev[s];
+    const int bounds[5] = {0, 4, 9, 13, 14};
     for (int p = 0; p < 4; p++)
-      if (cudaEventElapsedTime(&ms, b->pev[s][p], b->pev[s][p + 1]) == cudaSuccess) b->t_phase[p] += ms;
+      if (cudaEventElapsedTime(&ms, e[bounds[p]], e[bounds[p + 1]]) == cudaSuccess) b->t_phase[p] += ms;
+    for (int c = 0; c < kClasses; c++) {
+      if (cudaEventElapsedTime(&ms, e[c], e[1 + c]) == cudaSuccess) b->t_class[0][c] += ms;
+      if (cudaEventElapsedTime(&ms, e[4 + c], e[5 + c]) == cudaSuccess) b->t_class[1][c] += ms;
+      if (cudaEventElapsedTime(&ms, e[9 + c], e[10 + c]) == cudaSuccess) b->t_class[2][c] += ms;
+    }
+  }
 }
 
 int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
@@ -1025,7 +1037,10 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
   mark(b, slot, 0);
   for (int c = 0; c < kClasses; c++) {
     const int cnt = b->e_beg[c + 1] - b->e_beg[c];
-    if (!cnt) continue;
+    if (!cnt) {
+      mark(b, slot, 1 + c);
+      continue;
+    }
     const EItem *it0 = b->eitems + b->e_beg[c];
     double *ep = b->epart + b->e_beg[c];
     switch (c) {
@@ -1036,11 +1051,14 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     }
     FEM_CUDA(cudaGetLastError());
     b->launches++;
+    mark(b, slot, 1 + c);
   }
-  mark(b, slot, 1);
   for (int c = 0; c < kClasses; c++) {
     const int cnt = b->m_beg[c + 1] - b->m_beg[c];
-    if (!cnt) continue;
+    if (!cnt) {
+      mark(b, slot, 5 + c);
+      continue;
+    }
     const MItem *it0 = b->mitems + b->m_beg[c];
     switch (c) {
       case 0: k_b_means<4><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
@@ -1050,14 +1068,18 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     }
     FEM_CUDA(cudaGetLastError());
     b->launches++;
+    mark(b, slot, 5 + c);
   }
   k_b_final_means<128><<<b->nfits, 128, 0, b->stream>>>(fits, st, b->epart, b->mpart);
   FEM_CUDA(cudaGetLastError());
   b->launches++;
-  mark(b, slot, 2);
+  mark(b, slot, 9);
   for (int c = 0; c < kClasses; c++) {
     const int cnt = b->c_beg[c + 1] - b->c_beg[c];
-    if (!cnt) continue;
+    if (!cnt) {
+      mark(b, slot, 10 + c);
+      continue;
+    }
     const CItem *it0 = b->citems + b->c_beg[c];
     const size_t sm = b->c_smem[c];
     switch (c) {
@@ -1068,15 +1090,15 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     }
     FEM_CUDA(cudaGetLastError());
     b->launches++;
+    mark(b, slot, 10 + c);
   }
-  mark(b, slot, 3);
   k_b_factor<<<b->ncomps, kBFThreads, 0, b->stream>>>(fits, st, b->comps, b->cpart, b->cfg.reg_coef, 1, svd);
   FEM_CUDA(cudaGetLastError());
   k_b_sweep_end<<<1, 1024, 0, b->stream>>>(st, b->nfits, it, b->cfg.max_sweeps, b->cfg.eps, b->cfg.abort_thr, svd,
                                            b->trace, b->etrace, b->cap, b->nactive);
   FEM_CUDA(cudaGetLastError());
   b->launches += 2;
-  mark(b, slot, 4);
+  mark(b, slot, 14);
   return FEM_OK;
 }
 
@@ -1445,6 +1467,8 @@ extern "C" int fem_em_batch_timing_enable(fem_em_batch *b, int on) {
   FEM_TRY(check_batch(b));
   b->timing = on != 0;
   for (double &t : b->t_phase) t = 0.0;
+  for (auto &row : b->t_class)
+    for (double &t : row) t = 0.0;
   b->launches = 0;
   b->sweeps = 0;
   return FEM_OK;
@@ -1456,5 +1480,16 @@ extern "C" int fem_em_batch_timing(fem_em_batch *b, double *phase_ms, int64_t *l
     for (int p = 0; p < 5; p++) phase_ms[p] = b->t_phase[p];
   if (launches) *launches = b->launches;
   if (sweeps) *sweeps = b->sweeps;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_timing_classes(fem_em_batch *b, double *class_ms) {
+  FEM_TRY(check_batch(b));
+  if (!class_ms) {
+    set_error("null output");
+    return FEM_ERR_BAD_ARG;
+  }
+  for (int p = 0; p < 3; p++)
+    for (int c = 0; c < kClasses; c++) class_ms[p * kClasses + c] = b->t_class[p][c];
   return FEM_OK;
 }

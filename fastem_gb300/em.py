@@ -47,7 +47,7 @@ class GaussianMixture:
 class CudaMatrixEM:
     """EMAlgorithm with every sweep on the GPU.
 
-    precision: "mixed" (tcgen05 BF16 contractions, FP32 accumulation, FP64
+    precision: "mixed" (tcgen05 FP16 hi/lo split contractions, FP32 accumulation, FP64
     factorisation / logdet / logL), "fp32" (CUDA cores) or "fp64"."""
 
     def __init__(self, ncols, nrows, ncl, precision="mixed", device=0, svd=False):

@@ -48,7 +48,7 @@ typedef enum fem_status {
 typedef enum fem_precision {
   FEM_PREC_FP64 = 0,  /* whole iteration in FP64, like the reference's double build */
   FEM_PREC_FP32 = 1,  /* whole iteration in FP32 on CUDA cores (plain baseline) */
-  FEM_PREC_MIXED = 2  /* tcgen05 BF16 contractions, FP32 accumulate, FP64 Cholesky/logdet/logL */
+  FEM_PREC_MIXED = 2  /* tcgen05 FP16 hi/lo split contractions, FP32 accumulate, FP64 Cholesky/logdet/logL */
 } fem_precision;
 
 /* returns FEM_API_VERSION */
@@ -186,13 +186,16 @@ int fem_em_batch_fail_component(fem_em_batch *b, int fit, int *component);
  * [4] the whole sweep loop; kernel launches and sweeps since enabling */
 int fem_em_batch_timing_enable(fem_em_batch *b, int on);
 int fem_em_batch_timing(fem_em_batch *b, double *phase_ms, int64_t *launches, int64_t *sweeps);
+/* the E-step, means and covariance launches of each dimension class (d <= 4, 8, 16,
+ * 32) since enabling: class_ms[3 * 4], [phase * 4 + class] (ms, CUDA events) */
+int fem_em_batch_timing_classes(fem_em_batch *b, double *class_ms);
 
 /* ============================== k-means ============================== */
 
 typedef struct fem_km fem_km;
 
 typedef struct fem_km_config {
-  int precision;   /* FEM_PREC_FP32 (CUDA-core distances) or FEM_PREC_MIXED (tcgen05 BF16) */
+  int precision;   /* FEM_PREC_FP32 (CUDA-core distances) or FEM_PREC_MIXED (tcgen05, FP16 hi/lo splits) */
   int device;
   uint64_t seed;   /* seed of the repair RNG (Util/Rand.cpp SRand) */
   int repair;      /* 1: CentroidRandomRepair (Clust/CentroidRepair.cpp:21-28); 0: leave empty */
