@@ -548,6 +548,10 @@ def run_batched(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+KM_METRIC = "k-means iter/s N=2^24 d=32 K=256 (labels bit-exact to FP64)"
+KM_PROFILE_FILE = os.path.join(ROOT, "profiles", "kmeans_assign_n16m_d32_k256.md")
+
+
 def km_workload(n, d, k):
     from fastem_gb300 import synth
     X, _ = synth.kmeans_blobs(seed=2, n=n, d=d, k=k)

@@ -40,6 +40,7 @@ EXPORTS = [
     "fem_em_batch_timing_classes",
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
+    "fem_km_correct_without_mse",
     "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
     "fem_km_classify_noalloc",
 ]
@@ -128,6 +129,7 @@ def lib():
         "fem_km_upload_device": ([P, P, i64], i32),
         "fem_km_init_data_structures": ([P], i32),
         "fem_km_compute_mse_and_correct": ([P, P, P, P], i32),
+        "fem_km_correct_without_mse": ([P, P, P], i32),
         "fem_km_run": ([P, P, f64, i32, P, P], i32),
         "fem_km_get_assignment": ([P, P], i32),
         "fem_km_seed": ([P, ctypes.c_uint64], i32),

@@ -82,6 +82,8 @@ struct DevStatus {
   int timeout;         // a bounded wait gave up (mixed-precision kernels)
   int64_t rechecked;   // k-means rows re-decided in FP64
   double fit;          // k-means sum of squared distances
+  int track_changes;   // k-means: compare each new label with the stored one (set by the host)
+  int changed;         // k-means: some label differs from the stored one
 };
 
 // ------------------------------------------------------------------ EM handle

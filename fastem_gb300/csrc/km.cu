@@ -201,6 +201,7 @@ k_km_assign_f32(const float *__restrict__ X, int64_t n, int K, const float *__re
           }
         }
       }
+      if (st->track_changes && labels[base + tid] != lab) st->changed = 1;
       labels[base + tid] = lab;
       atomicAdd(&sCnt[lab], 1);
     }
@@ -491,7 +492,10 @@ int fem_km_seed(fem_km *h, uint64_t seed) {
   return FEM_OK;
 }
 
-int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, int64_t *counts) {
+// one Lloyd iteration (NaiveKMA::ComputeMSEAndCorrect / CorrectWithoutMSE,
+// Clust/KMAlgorithm.cpp:148-255): labels, fixed-point sums, divide or repair;
+// with `changed` the kernels also report whether any label moved
+static int km_iterate(fem_km *h, double *centroids, double *fit, int64_t *counts, int *changed) {
   FEM_TRY(check(h));
   if (!h->have_data || !centroids) {
     set_error("k-means iteration needs an uploaded dataset and centroids");
@@ -501,6 +505,7 @@ int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, in
   const int K = h->k, d = h->d;
   const size_t kd = (size_t)K * d;
   DevStatus z{};
+  z.track_changes = changed != nullptr;
   *h->hstat = z;
   FEM_CUDA(cudaMemcpyAsync(h->dstat, h->hstat, sizeof(DevStatus), cudaMemcpyHostToDevice, h->stream));
   FEM_CUDA(cudaMemcpyAsync(h->cent, centroids, kd * 8, cudaMemcpyHostToDevice, h->stream));
@@ -544,7 +549,20 @@ int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, in
       for (int q = 0; q < d; q++) centroids[(size_t)j * d + q] = (double)row[q];
     }
   }
+  if (changed) *changed = h->hstat->changed;
   return FEM_OK;
+}
+
+int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, int64_t *counts) {
+  return km_iterate(h, centroids, fit, counts, nullptr);
+}
+
+int fem_km_correct_without_mse(fem_km *h, double *centroids, int *changed) {
+  if (!changed) {
+    set_error("fem_km_correct_without_mse: null output");
+    return FEM_ERR_BAD_ARG;
+  }
+  return km_iterate(h, centroids, nullptr, nullptr, changed);
 }
 
 int fem_km_run(fem_km *h, double *centroids, double min_rel, int max_iter, double *best_fit, int *iters) {

@@ -405,6 +405,7 @@ k_km_assign_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__
             lab = db < da ? jb : ja;
           }
         }
+        if (st->track_changes && labels[row] != lab) st->changed = 1;
         labels[row] = lab;
         atomicAdd(&S.cnt[lab], 1);
         long long *accr = S.acc + lab * kKmAccPitch;

@@ -5,8 +5,9 @@
 //          [-f eps] [-a abort] [-g regcoeff] [-S] [-v verbosity]
 //          [-o mixture.cmp] [-O classes.bin] [-p mixed|fp32|fp64] [-d device]
 //   em2gpu --info file     (header and checksum of a .bin or .cmp file; no GPU)
+//   em2gpu --seed pp|oror file.bin K seed   (k-means++ / k-means|| centroids; no GPU)
 //
-// init (-I): jain (default), kmeans, or a .cmp file (EM2/EMInitializer.cpp:168-177).
+// init (-I): jain (default), kmeans, kmeansoror, or a .cmp file (EM2/EMInitializer.cpp:168-177).
 // -o writes the fitted mixture (.cmp), -O the classes of every row under the
 // fitted mixture, 1-based, after an int32 row count (GaussianMixture::WriteClasses).
 #include <chrono>
@@ -26,7 +27,7 @@ void usage() {
   std::printf(
       "Arguments: filename - name of the file in .bin format\n"
       "-c components : number of Gaussian mixture components\n"
-      "-I init : jain, kmeans or a .cmp file with the initial mixture\n"
+      "-I init : jain, kmeans, kmeansoror or a .cmp file with the initial mixture\n"
       "-r seed : seed of the pseudo-random number generator\n"
       "-m emiter : maximal number of EM iterations\n"
       "-b burnin : number of burn-in EM iterations (default 0)\n"
@@ -39,7 +40,8 @@ void usage() {
       "-O file : writes the classes of every row (int32 count, then 1-based classes)\n"
       "-p precision : mixed (default), fp32 or fp64\n"
       "-d device : CUDA device\n"
-      "--info file : prints the header and a checksum of a .bin or .cmp file\n");
+      "--info file : prints the header and a checksum of a .bin or .cmp file\n"
+      "--seed pp|oror file K seed : prints k-means++ / k-means|| centroids of a .bin file\n");
 }
 
 int info(const char *fname) {
@@ -65,7 +67,31 @@ int info(const char *fname) {
 
 }  // namespace
 
+// the seeders on the host (no GPU): K rows of %.17g coordinates
+static int seed_centroids(const char *how, const char *fname, int K, unsigned seed) {
+  Dataset D = Dataset::Load(fname);
+  Rand rnd(seed);
+  std::vector<double> C;
+  if (!std::strcmp(how, "pp")) C = KMeansPlusPlus(D, K, rnd, 0);
+  else if (!std::strcmp(how, "oror")) C = KMeansOrOr(D, K, rnd, 1.4);
+  else throw std::invalid_argument("--seed takes pp or oror");
+  const int d = D.GetColCount();
+  for (int j = 0; j < K; j++) {
+    for (int q = 0; q < d; q++) std::printf(q ? " %.17g" : "%.17g", C[(size_t)j * d + q]);
+    std::printf("\n");
+  }
+  return 0;
+}
+
 int main(int argc, char *argv[]) {
+  if (argc >= 6 && !std::strcmp(argv[1], "--seed")) {
+    try {
+      return seed_centroids(argv[2], argv[3], std::atoi(argv[4]), (unsigned)std::strtoul(argv[5], nullptr, 10));
+    } catch (std::exception &e) {
+      std::fprintf(stderr, "%s\n", e.what());
+      return 1;
+    }
+  }
   if (argc >= 3 && !std::strcmp(argv[1], "--info")) {
     try {
       return info(argv[2]);

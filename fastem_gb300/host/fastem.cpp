@@ -337,43 +337,149 @@ void CudaKMeans::Assignment(std::vector<int32_t> &labels) const {
 std::vector<double> KMeansPlusPlus(const Dataset &data, int K, Rand &rnd, int64_t sample) {
   const int64_t N = data.GetRowCount();
   const int d = data.GetColCount();
-  const int64_t S = (sample <= 0 || sample >= N) ? N : sample;
-  auto row = [&](int64_t s) { return data.GetRow(S == N ? s : s * (N / S)); };
-  std::vector<double> C((size_t)K * d), D2(S, DBL_MAX);
-  auto take = [&](int j, int64_t s) {
-    for (int q = 0; q < d; q++) C[(size_t)j * d + q] = row(s)[q];
-  };
-  take(0, std::min<int64_t>(S - 1, (int64_t)(rnd() * (double)S)));
-  for (int j = 1; j <= K; j++) {
-    // distances to centroid j - 1, then D^2 sampling of centroid j
+  if (sample <= 0 || sample >= N) return WeightedPlusPlus(data.GetRow(0), N, d, nullptr, K, rnd);
+  // `sample` rows spread evenly over the dataset
+  std::vector<float> P((size_t)sample * d);
+  for (int64_t s = 0; s < sample; s++)
+    std::copy(data.GetRow(s * (N / sample)), data.GetRow(s * (N / sample)) + d, P.begin() + (size_t)s * d);
+  return WeightedPlusPlus(P.data(), sample, d, nullptr, K, rnd);
+}
+
+std::vector<double> WeightedPlusPlus(const float *P, int64_t M, int d, const double *w, int K, Rand &rnd) {
+  std::vector<double> C((size_t)K * d, 0.0), best(M, DBL_MAX), agg(M);
+  const int64_t first = std::min<int64_t>(M - 1, (int64_t)(rnd() * (double)M));
+  for (int q = 0; q < d; q++) C[q] = P[(size_t)first * d + q];
+  for (int j = 1; j < K; j++) {
     const double *c = C.data() + (size_t)(j - 1) * d;
-    parallel_rows(S, [&](int64_t b, int64_t e, int) {
-      for (int64_t s = b; s < e; s++) {
-        double t = 0.0;
+    parallel_rows(M, [&](int64_t b, int64_t e, int) {
+      for (int64_t m = b; m < e; m++) {
+        double s = 0.0;
         for (int q = 0; q < d; q++) {
-          const double u = (double)row(s)[q] - c[q];
-          t += u * u;
+          const double t = c[q] - (double)P[(size_t)m * d + q];
+          s += t * t;
         }
-        D2[s] = std::min(D2[s], t);
+        best[m] = std::min(best[m], s);
       }
     });
-    if (j == K) break;
-    double tot = 0.0;
-    for (int64_t s = 0; s < S; s++) tot += D2[s];
-    const double target = rnd() * tot;
-    double acc = 0.0;
-    int64_t pick = S - 1;
-    for (int64_t s = 0; s < S; s++) {
-      acc += D2[s];
-      if (acc > target) {
-        pick = s;
+    double sum = 0.0;
+    for (int64_t m = 0; m < M; m++) {
+      sum += best[m] * (w ? w[m] : 1.0);
+      agg[m] = sum;
+    }
+    for (int64_t m = 0; m < M; m++) agg[m] /= sum;
+    const double r = rnd();
+    for (int64_t m = 0; m < M; m++)
+      if (r <= agg[m]) {
+        for (int q = 0; q < d; q++) C[(size_t)j * d + q] = P[(size_t)m * d + q];
         break;
       }
-    }
-    take(j, pick);
   }
   return C;
 }
+
+std::vector<double> KMeansOrOr(const Dataset &data, int K, Rand &rnd, double oversample) {
+  const int64_t N = data.GetRowCount();
+  const int d = data.GetColCount();
+  const int rounds = oversample <= 0.1 ? 10 : 5;
+  std::vector<double> best(N, DBL_MAX);
+  std::vector<int> owner(N, -1);
+  std::vector<float> cand;   // candidate rows, C x d
+  // squared distance of two float rows: per-coordinate terms in float, summed in double
+  auto dist = [d](const float *a, const float *b) {
+    double s = 0.0;
+    for (int q = 0; q < d; q++) {
+      const float t = b[q] - a[q];
+      s += (double)(t * t);
+    }
+    return s;
+  };
+  auto add = [&](const std::vector<float> &nc) {
+    const int base = (int)(cand.size() / d), m = (int)(nc.size() / d);
+    parallel_rows(N, [&](int64_t b, int64_t e, int) {
+      for (int64_t i = b; i < e; i++) {
+        const float *row = data.GetRow(i);
+        for (int j = 0; j < m; j++) {
+          const double s = dist(&nc[(size_t)j * d], row);
+          if (s < best[i]) {
+            best[i] = s;
+            owner[i] = base + j;
+          }
+        }
+      }
+    });
+    cand.insert(cand.end(), nc.begin(), nc.end());
+  };
+  auto cost = [&]() {
+    double s = 0.0;
+    for (int64_t i = 0; i < N; i++) s += best[i];
+    return s;
+  };
+  const int64_t first = std::min<int64_t>(N - 1, (int64_t)(rnd() * (double)N));
+  add(std::vector<float>(data.GetRow(first), data.GetRow(first) + d));
+  double c = cost();
+  for (int r = 0; r < rounds; r++) {
+    // one pass in row order, so the generator is consumed as by the reference on one thread
+    std::vector<float> nc;
+    for (int64_t i = 0; i < N; i++)
+      if (rnd() < oversample * (double)K * best[i] / c) nc.insert(nc.end(), data.GetRow(i), data.GetRow(i) + d);
+    add(nc);
+    c = cost();
+  }
+  const int64_t M = (int64_t)(cand.size() / d);
+  std::vector<double> w(M, 0.0);
+  for (int64_t i = 0; i < N; i++) w[owner[i]] += 1.0;
+  return WeightedPlusPlus(cand.data(), M, d, w.data(), K, rnd);
+}
+
+namespace {
+
+// KMeansEMInitializer::Init after the seeding (EM2/EMInitializer.cpp:103-134):
+// 30 k-means iterations with MinRel 1e-4 on the GPU, the classes of the final
+// centroids, then the class covariances (divided by count - 1) and weights
+GaussianMixture MixtureFromCentroids(const Dataset &data, std::vector<double> C, int K, int precision,
+                                     int device) {
+  const int64_t N = data.GetRowCount();
+  const int d = data.GetColCount();
+  std::vector<int32_t> lab;
+  {
+    const int kprec = (precision == FEM_PREC_MIXED && d == 32) ? FEM_PREC_MIXED : FEM_PREC_FP32;
+    CudaKMeans km(data, K, kprec, device, 0, true);
+    km.RunKMeans(C, 0, 1e-4, 30);
+    // the classes of the final centroids (ClassifyDataset): one more assignment
+    std::vector<double> C2 = C;
+    km.ComputeMSEAndCorrect(C2);
+    km.Assignment(lab);
+  }
+  const int nt = host_threads();
+  std::vector<double> cs((size_t)nt * K * d * d, 0.0);
+  std::vector<int64_t> cnt((size_t)nt * K, 0);
+  parallel_rows(N, [&](int64_t b, int64_t e, int t) {
+    std::vector<double> r(d);
+    for (int64_t i = b; i < e; i++) {
+      const int c = lab[i];
+      cnt[(size_t)t * K + c]++;
+      for (int q = 0; q < d; q++) r[q] = (double)data.GetRow(i)[q] - C[(size_t)c * d + q];
+      double *S = cs.data() + ((size_t)t * K + c) * d * d;
+      for (int a = 0; a < d; a++)
+        for (int q = 0; q < d; q++) S[(size_t)a * d + q] += r[a] * r[q];
+    }
+  });
+  GaussianMixture G(K, d);
+  for (int j = 0; j < K; j++) {
+    int64_t n = 0;
+    for (int t = 0; t < nt; t++) n += cnt[(size_t)t * K + j];
+    for (size_t e = 0; e < (size_t)d * d; e++) {
+      double s = 0.0;
+      for (int t = 0; t < nt; t++) s += cs[((size_t)t * K + j) * d * d + e];
+      G.Covs()[(size_t)j * d * d + e] = s / ((double)n - 1.0);
+    }
+    for (int q = 0; q < d; q++) G.Means()[(size_t)j * d + q] = C[(size_t)j * d + q];
+    G.Weights()[j] = (double)n / (double)N;
+  }
+  return G;
+}
+
+}  // namespace
 
 GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &rnd, int precision, int device) {
   const int64_t N = data.GetRowCount();
@@ -398,49 +504,14 @@ GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &
   }
   if (!std::strcmp(name, "kmeans")) {
     // KMeansEMInitializer: k-means++ centroids (D^2 sampling over at most
-    // 2^18 evenly spread rows), 30 k-means iterations with MinRel 1e-4 on the
-    // GPU, then the class covariances (divided by count - 1) and class weights
-    std::vector<double> C = KMeansPlusPlus(data, K, rnd, 1 << 18);
-    std::vector<int32_t> lab;
-    {
-      const int kprec = (precision == FEM_PREC_MIXED && d == 32) ? FEM_PREC_MIXED : FEM_PREC_FP32;
-      CudaKMeans km(data, K, kprec, device, 0, true);
-      km.RunKMeans(C, 0, 1e-4, 30);
-      // the classes of the final centroids (ClassifyDataset): one more assignment
-      std::vector<double> C2 = C;
-      km.ComputeMSEAndCorrect(C2);
-      km.Assignment(lab);
-    }
-    const int nt = host_threads();
-    std::vector<double> cs((size_t)nt * K * d * d, 0.0);
-    std::vector<int64_t> cnt((size_t)nt * K, 0);
-    parallel_rows(N, [&](int64_t b, int64_t e, int t) {
-      std::vector<double> r(d);
-      for (int64_t i = b; i < e; i++) {
-        const int c = lab[i];
-        cnt[(size_t)t * K + c]++;
-        for (int q = 0; q < d; q++) r[q] = (double)data.GetRow(i)[q] - C[(size_t)c * d + q];
-        double *S = cs.data() + ((size_t)t * K + c) * d * d;
-        for (int a = 0; a < d; a++)
-          for (int q = 0; q < d; q++) S[(size_t)a * d + q] += r[a] * r[q];
-      }
-    });
-    GaussianMixture G(K, d);
-    for (int j = 0; j < K; j++) {
-      int64_t n = 0;
-      for (int t = 0; t < nt; t++) n += cnt[(size_t)t * K + j];
-      for (size_t e = 0; e < (size_t)d * d; e++) {
-        double s = 0.0;
-        for (int t = 0; t < nt; t++) s += cs[((size_t)t * K + j) * d * d + e];
-        G.Covs()[(size_t)j * d * d + e] = s / ((double)n - 1.0);
-      }
-      for (int q = 0; q < d; q++) G.Means()[(size_t)j * d + q] = C[(size_t)j * d + q];
-      G.Weights()[j] = (double)n / (double)N;
-    }
-    return G;
+    // 2^18 evenly spread rows), then k-means and class covariances
+    return MixtureFromCentroids(data, KMeansPlusPlus(data, K, rnd, 1 << 18), K, precision, device);
   }
-  if (!std::strcmp(name, "kmeansoror"))
-    throw std::invalid_argument("the k-means|| EM initializer is not built in this backend; use kmeans or a file");
+  if (!std::strcmp(name, "kmeansoror")) {
+    // KMeansOrOrEMInitializer (EM2/EMInitializer.cpp:153-157): k-means||
+    // centroids with oversampling 1.4, then as above
+    return MixtureFromCentroids(data, KMeansOrOr(data, K, rnd, 1.4), K, precision, device);
+  }
   return GaussianMixture::Read(name);
 }
 

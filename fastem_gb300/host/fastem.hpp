@@ -160,9 +160,18 @@ class Rand {
 };
 
 // k-means++ centroids (Clust/PlusPlusInitializer/PlusPlusInitializer.cpp:33-83),
-// FP64 on the host over `sample` rows spread evenly over the dataset (all rows
-// if sample <= 0 or >= N)
+// FP64 on the host over `sample` rows spread evenly over the dataset (all rows,
+// as the reference, if sample <= 0 or >= N)
 std::vector<double> KMeansPlusPlus(const Dataset &data, int K, Rand &rnd, int64_t sample = 0);
+// weighted k-means++ over M candidate rows P (PlusPlusInitializer with
+// SetWeights: first row uniform, then D^2 w sampling), w may be null
+std::vector<double> WeightedPlusPlus(const float *P, int64_t M, int d, const double *w, int K, Rand &rnd);
+// k-means|| centroids (Clust/KMeansOrOrInitializer.cpp:143-174): a random first
+// row, 5 rounds (10 if oversample <= 0.1) sampling each row with probability
+// oversample K D^2 / cost, the candidates weighted by the rows closest to them,
+// then weighted k-means++ down to K.  The sampling pass draws in row order (the
+// reference's multi-threaded pass shares one generator between threads)
+std::vector<double> KMeansOrOr(const Dataset &data, int K, Rand &rnd, double oversample = 1.4);
 // initial mixture by name: "jain", "kmeans", "kmeansoror" or a .cmp file
 // (CreateEMInitializer, EM2/EMInitializer.cpp:168-177)
 GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &rnd, int precision = FEM_PREC_MIXED,

@@ -70,6 +70,15 @@ class CudaKMA:
                                                        None))
         return fit.value
 
+    def CorrectWithoutMSE(self, vec):
+        """NaiveKMA::CorrectWithoutMSE (Clust/KMAlgorithm.cpp:148-202): vec
+        updated in place; True when some label changed since the previous
+        iteration."""
+        assert vec.dtype == np.float64 and vec.flags.c_contiguous
+        changed = ctypes.c_int(0)
+        C.check(C.lib().fem_km_correct_without_mse(self._h, C.ptr(vec), ctypes.byref(changed)))
+        return bool(changed.value)
+
     def ComputeMSEAndCorrectCounts(self, vec):
         assert vec.dtype == np.float64 and vec.flags.c_contiguous
         fit = ctypes.c_double(np.nan)

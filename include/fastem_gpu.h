@@ -217,6 +217,11 @@ int fem_km_init_data_structures(fem_km *h);
  * NULL.  Assignments are bit-exact to an FP64 difference-form argmin with
  * the lowest index winning ties. */
 int fem_km_compute_mse_and_correct(fem_km *h, double *centroids, double *fit, int64_t *counts);
+/* NaiveKMA::CorrectWithoutMSE (Clust/KMAlgorithm.cpp:148-202): the same
+ * iteration without the fit; *changed = 1 when some point's label differs
+ * from the one stored by the previous iteration (all zero after
+ * fem_km_init_data_structures, like Assignment[]) */
+int fem_km_correct_without_mse(fem_km *h, double *centroids, int *changed);
 /* KMeansAlgorithm::RunKMeans (Clust/KMAlgorithm.cpp:44-87) */
 int fem_km_run(fem_km *h, double *centroids, double min_rel, int max_iter, double *best_fit,
                int *iters);

@@ -123,3 +123,28 @@ def test_em2gpu_kmeans_init_mixed_and_unsupported_width(em2gpu, tmp_path):
     bad = subprocess.run([em2gpu, fw, "-c", "4", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
                          timeout=300)
     assert bad.returncode == 1 and "mixed precision" in bad.stderr
+    # the k-means|| EM initializer (KMeansOrOrEMInitializer)
+    oror = subprocess.run([em2gpu, fb, "-c", "6", "-I", "kmeansoror", "-p", "fp32", "-m", "5", "-r", "7"],
+                          capture_output=True, text=True, timeout=300)
+    assert oror.returncode == 0, oror.stdout + oror.stderr
+    assert np.isfinite(float(oror.stdout.split("Final loglikelihood:")[1].split()[0]))
+
+
+def seed(exe, how, fname, k, s):
+    out = subprocess.run([exe, "--seed", how, fname, str(k), str(s)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    return np.array([[float(v) for v in ln.split()] for ln in out.stdout.strip().splitlines()])
+
+
+@pytest.mark.parametrize("how,n,d,k,s", [("pp", 5000, 8, 10, 2), ("oror", 20000, 16, 12, 3), ("oror", 3000, 5, 40, 7)])
+def test_host_seeders_match_oracle(em2gpu, oracle, tmp_path, how, n, d, k, s):
+    """k-means++ and k-means|| in the C++ host library (the -I kmeans /
+    kmeansoror initialisers) pick the same rows as the oracle's restatement of
+    PlusPlusInitializer / KMeansOrOrInitializer from the same generator seed."""
+    X, _ = synth.kmeans_blobs(seed=30 + s, n=n, d=d, k=k, spread=5.0)
+    f = str(tmp_path / "x.bin")
+    formats.write_bin(f, X)
+    got = seed(em2gpu, how, f, k, s)
+    ref = oracle.kmeans_plusplus(X, k, seed=s) if how == "pp" else oracle.kmeans_oror(X, k, seed=s)
+    assert got.shape == (k, d)
+    np.testing.assert_array_equal(got, ref)

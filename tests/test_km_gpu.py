@@ -142,3 +142,27 @@ def test_km_tc_far_from_origin(gpu_lib, oracle):
     out = iterate_both(oracle, X, C0, 4, "mixed", repair=False)
     check_iters(out)
     print("rechecked rows per iteration:", [o[-1]["rechecked"] for o in out])
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_km_correct_without_mse(gpu_lib, oracle, precision):
+    """NaiveKMA::CorrectWithoutMSE: the same iteration without the fit,
+    reporting whether any label changed since the previous one (all zero
+    before the first); run until nothing changes, as KMeansWithoutMSE does."""
+    X, _ = synth.kmeans_blobs(seed=11, n=20000, d=32, k=12, spread=6.0)
+    C0 = X[np.random.default_rng(3).choice(len(X), 12, replace=False)].astype(np.float64)
+    Cg, Co = C0.copy(), C0.copy()
+    prev = np.zeros(len(X), dtype=np.int32)
+    with CudaKMA(32, len(X), 12, precision=precision, repair=True) as km:
+        km.SetDataset(X)
+        km.InitDataStructures()
+        for it in range(60):
+            changed = km.CorrectWithoutMSE(Cg)
+            _, Co, _, lo = oracle.km_iterate(X, Co, repair=True)
+            assert np.array_equal(km.Assignment(), lo), it
+            np.testing.assert_allclose(Cg, Co, rtol=1e-13, atol=1e-13)
+            assert changed == bool(np.any(lo != prev)), it
+            prev = lo.copy()
+            if not changed:
+                break
+        assert not changed and it > 1
