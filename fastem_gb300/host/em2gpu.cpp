@@ -40,6 +40,7 @@ void usage() {
       "-O file : writes the classes of every row (int32 count, then 1-based classes)\n"
       "-p precision : mixed (default), fp32 or fp64\n"
       "-d device : CUDA device\n"
+      "-A/-R/-M/-N/-T/-t/-u/-U : the reference's CPU tuning options, accepted and ignored\n"
       "--info file : prints the header and a checksum of a .bin or .cmp file\n"
       "--seed pp|oror file K seed : prints k-means++ / k-means|| centroids of a .bin file\n");
 }
@@ -106,8 +107,33 @@ int main(int argc, char *argv[]) {
   bool svd = true;
   const char *iname = nullptr, *oname = nullptr, *cname = nullptr;
   int c;
-  while ((c = getopt(argc, argv, "c:I:r:m:b:f:a:g:Sv:o:O:p:d:h")) != -1) {
+  while ((c = getopt(argc, argv, "c:I:r:m:b:f:a:g:Sv:o:O:p:d:hBN:M:A:R:T:t:u:U:")) != -1) {
     switch (c) {
+      // the reference's CPU tuning options (EM2/EMArgs.cpp:76-158): accepted so
+      // that em2 command lines run unchanged; they select OpenMP loop shapes,
+      // reducers and NUMA placement, which the GPU backend does not have
+      case 'N': {
+        // BlockManagerBase::ParseEMBlockParams (EM2/BlockManager.cpp:18-28)
+        double l3;
+        int a, b;
+        if (std::sscanf(optarg, "automax:%lf", &l3) != 1 && std::sscanf(optarg, "%d:%d", &a, &b) != 2) {
+          std::fprintf(stderr, "Bad value of MStepLoopParam\n");
+          return 1;
+        }
+        break;
+      }
+      case 'A':
+        // CreateEMAlgorithm's names (EM2/EMAlgorithm.cpp:247-269): all run on this backend
+        if (std::strcmp(optarg, "matrixem") && std::strcmp(optarg, "simplematrixem") &&
+            std::strcmp(optarg, "cachedem")) {
+          std::fprintf(stderr, "Invalid EM algorithm name %s\n", optarg);
+          return 1;
+        }
+        break;
+      case 'M': case 'R': case 'T': case 't': case 'u': case 'U': break;
+      case 'B':
+        std::printf("-B benchmarks the reference's OpenMP reduction; the GPU backend has none\n");
+        return 0;
       case 'c': ncl = std::atoi(optarg); break;
       case 'I': iname = optarg; break;
       case 'r': seed = (unsigned)std::atoi(optarg); break;

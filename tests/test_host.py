@@ -148,3 +148,19 @@ def test_host_seeders_match_oracle(em2gpu, oracle, tmp_path, how, n, d, k, s):
     ref = oracle.kmeans_plusplus(X, k, seed=s) if how == "pp" else oracle.kmeans_oror(X, k, seed=s)
     assert got.shape == (k, d)
     np.testing.assert_array_equal(got, ref)
+
+
+def test_em2gpu_accepts_reference_cpu_options(em2gpu):
+    """em2's CPU tuning options parse as in the reference (-N as
+    ParseEMBlockParams, -A as CreateEMAlgorithm's names); -B has no GPU
+    counterpart."""
+    def run(*a):
+        return subprocess.run([em2gpu, *a], capture_output=True, text=True, timeout=60)
+    bad_n = run("-N", "3:x", "missing.bin")
+    assert bad_n.returncode == 1 and "Bad value of MStepLoopParam" in bad_n.stderr
+    bad_a = run("-A", "nosuchem", "missing.bin")
+    assert bad_a.returncode == 1 and "Invalid EM algorithm name" in bad_a.stderr
+    assert run("-B").returncode == 0
+    # well-formed options get as far as opening the (missing) data file
+    ok = run("-N", "automax:32", "-A", "simplematrixem", "-R", "log2", "-M", "simple", "missing.bin")
+    assert ok.returncode != 0 and "MStepLoopParam" not in ok.stderr and "algorithm" not in ok.stderr
