@@ -408,11 +408,22 @@ k_km_assign_tc(const __grid_constant__ CUtensorMap tm_x, const __grid_constant__
         if (st->track_changes && labels[row] != lab) st->changed = 1;
         labels[row] = lab;
         atomicAdd(&S.cnt[lab], 1);
-        long long *accr = S.acc + lab * kKmAccPitch;
-#pragma unroll
-        for (int q = 0; q < kKmD; q++)
-          atomicAdd(reinterpret_cast<unsigned long long *>(accr + q),
-                    (unsigned long long)__float2ll_rn(xs[(((q >> 2) ^ (r & 7)) << 2) + (q & 3)] * scale));
+      }
+      // exact fixed-point sums, one row of the warp at a time: lane q adds
+      // dimension q, so each 64-bit atomic instruction updates 32 consecutive
+      // words of one centroid row (conflict-free) instead of 32 scattered rows
+      {
+        const int mylab = row < n ? lab : -1;
+#pragma unroll 4
+        for (int rr = 0; rr < 32; rr++) {
+          const int l = __shfl_sync(0xffffffffu, mylab, rr);
+          if (l >= 0) {
+            const int rq = quad * 32 + rr;
+            const float xv = S.x[s][rq * kKmD + ((((lane >> 2) ^ (rq & 7)) << 2) + (lane & 3))];
+            atomicAdd(reinterpret_cast<unsigned long long *>(S.acc + l * kKmAccPitch + lane),
+                      (unsigned long long)__float2ll_rn(xv * scale));
+          }
+        }
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&S.x_empty[s]);
