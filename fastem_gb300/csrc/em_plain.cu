@@ -275,6 +275,7 @@ __global__ void k_final_means(const double *__restrict__ part, int G, int K, int
 // z z^T over the upper block triangle.  Each thread owns one TB x TB block
 // of one component; a CTA owns 256 consecutive (component, block) units.
 constexpr int kCovTP = 32;
+constexpr int kCovFlushTiles = 64;   // FP32 sums span at most 64 tiles (2048 rows)
 
 // posterior (component j, point i): typed component-major array, or the
 // mixed path's FP16 hi + lo pair
@@ -325,6 +326,14 @@ k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T
 #pragma unroll
     for (int b = 0; b < TB; b++) acc[a][b] = T(0);
   const int cj = j - j_lo;
+  // this thread's FP64 partial block (owned by it alone): the FP32 sums are
+  // added into it every kCovFlushTiles tiles, so FP32 never sums more than
+  // 2048 rows (ill-conditioned covariances stay positive definite)
+  double *o = valid ? part + (((size_t)blockIdx.y * K + j) * nblk + (unit - j * nblk)) * (TB * TB) : nullptr;
+  if (valid)
+#pragma unroll
+    for (int e = 0; e < TB * TB; e++) o[e] = 0.0;
+  int tiles = 0;
   for (int64_t t0 = c0; t0 < c1; t0 += kCovTP) {
     const int tp = (int)min((int64_t)kCovTP, c1 - t0);
     __syncthreads();
@@ -356,14 +365,14 @@ k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T
 #pragma unroll
           for (int b = 0; b < TB; b++) acc[a][b] = fma(va[a], vb[b], acc[a][b]);
       }
+      if (++tiles == kCovFlushTiles || t0 + kCovTP >= c1) {
+        tiles = 0;
+#pragma unroll
+        for (int a = 0; a < TB; a++)
+#pragma unroll
+          for (int b = 0; b < TB; b++) o[a * TB + b] += (double)acc[a][b], acc[a][b] = T(0);
+      }
     }
-  }
-  if (valid) {
-    double *o = part + (((size_t)blockIdx.y * K + j) * nblk + (unit - j * nblk)) * (TB * TB);
-#pragma unroll
-    for (int a = 0; a < TB; a++)
-#pragma unroll
-      for (int b = 0; b < TB; b++) o[a * TB + b] = (double)acc[a][b];
   }
 }
 
