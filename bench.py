@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="em", choices=["em", "kmeans", "batched"])
+    ap.add_argument("--workload", default="em", choices=["em", "kmeans", "batched", "small", "illcond"])
     ap.add_argument("--n", type=int, default=None, help="points (default 2^23 EM, 2^24 k-means)")
     ap.add_argument("--k", type=int, default=128)
     ap.add_argument("--fits-d", type=int, default=None, choices=[4, 8, 16, 32],
@@ -166,16 +166,16 @@ def em_flops(n, d, k):
     return dict(estep=tri, cov=tri, mstep=tri + 2 * n * k * d, total=2 * tri + 2 * n * k * d)
 
 
-def time_device_sweeps(em, G, warmup, steps, dist):
+def time_device_sweeps(em, G, warmup, steps, dist, reg=0.0):
     """Warm-up sweeps, then `steps` sweeps timed by CUDA events on the
     library's stream (max over ranks)."""
     import torch
-    em.SetParameters(warmup, 0.0, 1e5)
+    em.SetParameters(warmup, 0.0, 1e5, reg)
     em.TrainNoCopy(G)
     dist.barrier()
     torch.cuda.synchronize()
     em.TimingReset(True)
-    em.SetParameters(steps, 0.0, 1e5)
+    em.SetParameters(steps, 0.0, 1e5, reg)
     em.TrainNoCopy(G)
     torch.cuda.synchronize()
     dist.barrier()
@@ -247,6 +247,12 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, rank, world, local)
+        return
+    if args.workload == "small":
+        run_small(args, rank, world, local)
+        return
+    if args.workload == "illcond":
+        run_illcond(args, rank, world, local)
         return
     if args.n is None:
         args.n = 1 << 23
@@ -375,20 +381,30 @@ def batched_workload():
     return fits, data
 
 
-def batched_cpu_baseline(fits, data, sample_every=32):
+def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None):
     """The oracle's TrainNoCopy (FP64, OpenMP over all host cores) on every
-    `sample_every`-th fit, 30 sweeps each."""
+    `sample_every`-th fit, 30 sweeps each.  With `gpu_traces` ({fit: LogL
+    trace}) the oracle's traces of the same fits check the GPU's:
+    the largest per-fit |dlogL/N|."""
     from oracle import oracle as O
     O.lib()
     idx = list(range(0, len(fits), sample_every))
     t0 = time.perf_counter()
+    refs = {}
     for i in idx:
         X, init = data[i]
-        O.em_train(X, *init, BATCH_SWEEPS, eps=0.0, abort_thr=1e12, nthreads=os.cpu_count())
+        refs[i] = O.em_train(X, *init, BATCH_SWEEPS, eps=0.0, abort_thr=1e12, nthreads=os.cpu_count())
     dt = time.perf_counter() - t0
+    errs = []
+    for i, tr in (gpu_traces or {}).items():
+        ref = refs.get(i)
+        if ref is not None and ref["status"] == 0:
+            m = min(len(tr), len(ref["logl"]))
+            errs.append(float(np.max(np.abs(tr[:m] - ref["logl"][:m])) / fits[i]["n"]))
     return {"value": len(idx) / dt, "unit": "fits/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d of the 512 fits (every %dth), %d sweeps each, %.1f s" % (len(idx), sample_every,
-                                                                                   BATCH_SWEEPS, dt)}
+            "sample": "%d of the %d fits (every %dth), %d sweeps each, %.1f s" % (len(idx), len(fits), sample_every,
+                                                                                 BATCH_SWEEPS, dt),
+            "max_dlogL_per_N_vs_gpu": max(errs) if errs else None, "checked_fits": len(errs)}
 
 
 def run_batched(args, rank, world, local):
@@ -489,19 +505,11 @@ def run_batched(args, rank, world, local):
             torch.cuda.synchronize()
             per_fit = {"value": nf / (time.perf_counter() - t0), "unit": "fits/s",
                        "scheme": "one FP32 handle and stream per fit, 16 host threads"}
-    errs, cpu = [], None
-    if not args.no_cpu and rank == 0:
-        from oracle import oracle as O
-        O.lib()
-        for i in range(0, nf, 64):
-            X, init = data[i]
-            ref = O.em_train(X, *init, BATCH_SWEEPS, eps=0.0, abort_thr=1e12)
-            if st[i] == 0 and ref["status"] == 0:
-                tr, _ = B.Trace(i)
-                m = min(len(tr), len(ref["logl"]))
-                errs.append(float(np.max(np.abs(tr[:m] - ref["logl"][:m])) / fits[i]["n"]))
-        if world == 1:
-            cpu = batched_cpu_baseline(fits, data)
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        # the CPU baseline leg also checks the sampled fits' LogL traces
+        traces = {i: B.Trace(i)[0] for i in range(0, nf, 32) if st[i] == 0}
+        cpu = batched_cpu_baseline(fits, data, gpu_traces=traces)
     B.close()
     dist.close()
     if rank != 0:
@@ -540,10 +548,232 @@ def run_batched(args, rank, world, local):
                      "peak_source": "nominal FP32 CUDA-core rate at the sampled SM clock (no measured FP32 peak)",
                      "traffic": traffic, "algorithmic_flop_per_step": cov_flop,
                      "launch_ms": cov_s * 1e3 / BATCH_SWEEPS},
-        "failed_fits": int((st != 0).sum()), "failed_fits_oracle_agrees": "fits 282, 283, 385 collapse in FP64",
-        "max_dlogL_per_N_sampled": max(errs) if errs else None, "sampled_fits": len(errs),
+        "failed_fits": int((st != 0).sum()),
+        "failed_fits_note": None if args.fits_d else "fits 282, 283, 385 also collapse in the FP64 oracle",
+        "max_dlogL_per_N_sampled": cpu["max_dlogL_per_N_vs_gpu"] if cpu else None,
+        "sampled_fits": cpu["checked_fits"] if cpu else 0,
         "per_fit_handles": per_fit, "speedup_vs_per_fit_handles": (value / per_fit["value"]) if per_fit else None,
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": tm["launches"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+SMALL_METRIC = "EM iter/s N=1e5 d=8 K=10 (FP64 sweeps, per-sweep logL against the FP64 oracle)"
+ILL_METRIC = "EM iter/s N=2^21 d=256 K=64, covariance condition 1e6 (FP64 CUDA cores; the FP32 form beside it)"
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64, nominal (no measured FP64 peak)
+ILL_REG = 1e-6               # RegCoef of the ill-conditioned workload (-g 1e-6)
+
+
+def l2_flush(buf):
+    """Writes a buffer larger than L2 (129 MB) on the current stream."""
+    buf.add_(1.0)
+
+
+def time_single_sweeps(em, G, steps, dist, flush):
+    """`steps` one-sweep trains, L2 flushed before each (outside the timed
+    events on the library's stream); returns the summed sweep-loop ms."""
+    import torch
+    em.TimingReset(True)
+    em.SetParameters(1, 0.0, 1e12)
+    for _ in range(steps):
+        flush()
+        torch.cuda.synchronize()
+        em.TrainNoCopy(G.copy())
+    torch.cuda.synchronize()
+    t = em.Timing()
+    em.TimingReset(False)
+    return dist.max(t["train_ms"]), t["launches"]
+
+
+def run_small(args, rank, world, local):
+    """N = 100,000, d = 8, K = 10 (em_small, seed 1): D^2-sampled means
+    (seed 2), identity covariances, uniform weights.  A step is one sweep;
+    `value` = FP64 sweeps/s (the reference's precision), FP32 and mixed
+    beside it.  The inputs (3.2 MB) fit in L2, so every timed sweep is its own
+    train call after an L2 flush.  The CPU baseline leg runs the oracle's 50
+    sweeps and checks the GPU's FP64 LogL trace against them."""
+    import torch
+    from fastem_gb300 import CudaMatrixEM, GaussianMixture, synth
+    from fastem_gb300 import _capi as C
+    X, _ = synth.em_small()
+    n, d, k = X.shape[0], X.shape[1], 10
+    init = synth.dsquared_init(X, k, seed=2)
+    if args.impl == "reference":
+        if rank == 0:
+            from oracle import oracle as O
+            O.lib()
+            t0 = time.perf_counter()
+            O.em_train(X, *init, 50, eps=0.0, abort_thr=1e12, nthreads=os.cpu_count())
+            v = 50 / (time.perf_counter() - t0)
+            cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": "50 sweeps, all rows"}
+            print(json.dumps({"metric": SMALL_METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": world,
+                              "steps": 50, "warmup": 0, "higher_is_better": True, "cpu_baseline": cpu,
+                              "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                              "config": {"workload": "em_small N=100000 d=8 K=10"}}), flush=True)
+        return
+    dist = Dist(world)
+    torch.cuda.set_device(local)
+    flush_buf = torch.zeros(128 << 20, dtype=torch.float32, device="cuda")   # 512 MB > L2
+    G = GaussianMixture(*init)
+    res, trace64 = {}, None
+    clocks = Clocks(local)
+    clocks.start()
+    for prec in ("fp64", "fp32", "mixed"):
+        with CudaMatrixEM(d, n, k, precision=prec, device=local) as em:
+            em.CopyDataset(X)
+            em.SetParameters(max(args.warmup, 3), 0.0, 1e12)
+            em.TrainNoCopy(G.copy())
+            ms, launches = time_single_sweeps(em, G, args.steps, dist, lambda: l2_flush(flush_buf))
+            res[prec] = {"value": world * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                         "launches": launches}
+            if prec == "fp64":
+                em.SetParameters(50, 0.0, 1e12)
+                Gt = G.copy()
+                em.TrainNoCopy(Gt)
+                trace64 = em.logl_trace.copy()
+                # end to end through the C-ABI: host rows -> device, parameters, one sweep, parameters back
+                steps = max(1, min(args.steps, 10))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(steps):
+                    C.check(C.lib().fem_em_upload(em.handle, C.ptr(C.f32rows(X)), d))
+                    em.SetParameters(1, 0.0, 1e12)
+                    Ge = G.copy()
+                    em.TrainNoCopy(Ge)
+                e2e = {"value": world * steps / dist.max(time.perf_counter() - t0), "unit": UNIT,
+                       "h2d_bytes_per_step": X.nbytes + k * (1 + d + d * d) * 8,
+                       "d2h_bytes_per_step": k * (1 + d + d * d) * 8}
+    clk = clocks.stop()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle as O
+        O.lib()
+        t0 = time.perf_counter()
+        ref = O.em_train(X, *init, 50, eps=0.0, abort_thr=1e12, nthreads=os.cpu_count())
+        dt = time.perf_counter() - t0
+        err = float(np.max(np.abs(trace64 - ref["logl"])) / n) if len(ref["logl"]) == len(trace64) else None
+        cpu = {"value": 50 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": "50 sweeps, all rows", "fp64_gpu_max_dlogL_per_N": err}
+    dist.close()
+    if rank != 0:
+        return
+    fl = em_flops(n, d, k)["total"]
+    ms = res["fp64"]["ms_per_step"]
+    achieved = fl / (ms / 1e3) / 1e12
+    line = {
+        "metric": SMALL_METRIC, "value": res["fp64"]["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic em_small (seeded: Dirichlet(1) weights, U[-10,10] means, A A^T + 0.5 I covariances)",
+        "config": {"workload": "em_small N=100000 d=8 K=10, one EM sweep per step", "n": n, "d": d, "k": k,
+                   "l2": "inputs 3.2 MB (below L2): 512 MB written between timed sweeps"},
+        "fp32": res["fp32"], "mixed": res["mixed"],
+        "roofline": {"kernel": "whole FP64 sweep", "bound": "fp64", "achieved": achieved,
+                     "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_NOMINAL_TFLOPS,
+                     "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak)", "traffic": None,
+                     "algorithmic_flop_per_step": fl, "note": "launch- and latency-bound at this size"},
+        "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": res["fp64"]["launches"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_illcond(args, rank, world, local):
+    """N = 2^21, d = 256, K = 64, eigenvalues log-spaced over [1e-3, 1e3]
+    (condition 1e6), Haar bases, N(0, 100 I) means (em_illcond, seed 5);
+    initial mixture = the generating one with means + 0.1 and covariances
+    x 1.05; run like the reference with -S (no condition check) and -g 1e-6
+    (RegCoef: with Dirichlet(1) weights some components hold fewer than 256
+    points, so their sample covariances are singular and the unregularised
+    fit stops with a Cholesky failure, in FP64 as in the reference).  `value` =
+    FP64 sweeps/s on the device (the reference's precision; the tensor-core
+    path covers d <= 64).  The FP32 CUDA-core form is run too and its outcome
+    reported: at this condition its covariance sums (FP32 over a point chunk)
+    lose positive definiteness.  Accuracy of FP32 against FP64 on the first
+    2^16 rows when FP32 gets through."""
+    import torch
+    from fastem_gb300 import CudaMatrixEM, GaussianMixture, synth
+    from fastem_gb300 import _capi as C
+    X, info = synth.em_illcond()
+    n, d, k = X.shape[0], X.shape[1], 64
+    init = (info["weights"], info["means"] + 0.1, info["covs"] * 1.05)
+    if args.impl == "reference":
+        if rank == 0:
+            sec, how = cpu_sweep_seconds(X, init, 1 << 13, os.cpu_count())
+            v = (1 << 13) / n / sec
+            cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                   "sample": "1 sweep (%s) over the first 8192 rows, scaled x%d" % (how, n >> 13)}
+            print(json.dumps({"metric": ILL_METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": world,
+                              "steps": 1, "warmup": 0, "higher_is_better": True, "cpu_baseline": cpu,
+                              "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                              "config": {"workload": "em_illcond N=2097152 d=256 K=64"}}), flush=True)
+        return
+    dist = Dist(world)
+    torch.cuda.set_device(local)
+    steps, warm = max(1, min(args.steps, 2)), max(args.warmup, 3)
+    G = GaussianMixture(*init)
+    clocks = Clocks(local)
+    clocks.start()
+    with CudaMatrixEM(d, n, k, precision="fp64", device=local) as em:
+        em.CopyDataset(X)
+        t = time_device_sweeps(em, G.copy(), warm, steps, dist, reg=ILL_REG)
+    clk = clocks.stop()
+    ms = dist.max(t["train_ms"]) / t["sweeps"]
+    value = world * 1e3 / ms
+    # the FP32 CUDA-core form at full size
+    fp32 = {}
+    with CudaMatrixEM(d, n, k, precision="fp32", device=local) as em:
+        em.CopyDataset(X)
+        em.SetParameters(warm + steps, 0.0, 1e12, ILL_REG)
+        em.TimingReset(True)
+        try:
+            em.TrainNoCopy(G.copy())
+            tt = em.Timing()
+            fp32 = {"status": "ok", "value": world * tt["sweeps"] / (tt["train_ms"] / 1e3)}
+        except C.FemError as e:
+            fp32 = {"status": str(e), "failed_at_sweep": em.GetIterCounter()}
+    # accuracy of FP32 against FP64, first 2^16 rows
+    m = 1 << 16
+    Xs = np.ascontiguousarray(X[:m])
+    tr, post, acc = {}, {}, {}
+    try:
+        for prec in ("fp64", "fp32"):
+            with CudaMatrixEM(d, m, k, precision=prec, device=local) as em:
+                em.SetParameters(3, 0.0, 1e12, ILL_REG)
+                em.Train(Xs, G.copy())
+                tr[prec] = em.logl_trace.copy()
+                post[prec] = em.Posteriors()
+        acc = {"rows": m, "sweeps": 3, "max_dlogL_per_N": float(np.max(np.abs(tr["fp32"] - tr["fp64"])) / m),
+               "max_dposterior": float(np.max(np.abs(post["fp32"] - post["fp64"])))}
+    except C.FemError as e:
+        acc = {"rows": m, "status": str(e)}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sec, how = cpu_sweep_seconds(X, init, 1 << 13, os.cpu_count())
+        cpu = {"value": (1 << 13) / n / sec, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": "1 sweep (%s) over the first 8192 rows, scaled x%d" % (how, n >> 13)}
+    dist.close()
+    if rank != 0:
+        return
+    fl = em_flops(n, d, k)["total"]
+    achieved = fl / (ms / 1e3) / 1e12
+    line = {
+        "metric": ILL_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": t["sweeps"],
+        "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp64",
+        "data": "synthetic em_illcond (seeded; eigenvalues log-spaced [1e-3, 1e3], Haar bases, N(0,100 I) means)",
+        "config": {"workload": "em_illcond N=2097152 d=256 K=64, one EM sweep per step", "n": n, "d": d, "k": k,
+                   "init": "generating mixture, means + 0.1, covariances x 1.05", "svd": "off (-S)",
+                   "reg_coef": ILL_REG,
+                   "l2": "inputs larger than L2 (X 2.1 GB, posteriors 1.1 GB)"},
+        "fp32": fp32, "accuracy_fp32_vs_fp64": acc,
+        "mixed": {"unavailable": "the tensor-core path covers d <= 64"},
+        "phase_ms_per_step": {"estep_ms": t["estep_ms"] / t["sweeps"], "mstep_ms": t["mstep_ms"] / t["sweeps"],
+                              "factor_ms": t["factor_ms"] / t["sweeps"]},
+        "roofline": {"kernel": "whole FP64 sweep", "bound": "fp64", "achieved": achieved,
+                     "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_NOMINAL_TFLOPS,
+                     "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak)", "traffic": None,
+                     "algorithmic_flop_per_step": fl},
+        "e2e": None, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": t["launches"],
     }
     print(json.dumps(line), flush=True)
 
