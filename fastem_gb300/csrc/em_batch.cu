@@ -49,7 +49,7 @@ constexpr int kBCThreads = 256;
 constexpr int kBFThreads = 256;
 constexpr int kBMChunk = 2048;   // points per means item
 constexpr int kBCChunk = 4096;   // points per covariance item
-constexpr int kBMTile = 32;      // points staged per means tile
+constexpr int kBMTile = 128;     // points staged per means tile
 constexpr int kBCTile = 16;      // points staged per covariance tile
 constexpr int kBatchSyncEvery = 8;
 constexpr int kTimeMarks = 15;   // timing events per sweep (see collect_timing)
@@ -322,18 +322,21 @@ k_b_estep(const BFit *__restrict__ fits, const BState *__restrict__ state, const
 // block of FP64 partials (column D holds PosteriorSum_j).  Threads own 4 x 4
 // micro-tiles of (component, column); when there are fewer micro-tiles than
 // threads, point groups split each tile's points and are summed at the end.
-// Tiles are loaded into registers one tile ahead.  FP32 sums over the item.
+// Tiles of kBMTile points are copied with cp.async one tile ahead into two
+// shared buffers (rows x (D + 4) with the ones column, posteriors point-major
+// with an odd stride).  FP32 sums over the item.
+template <int D>
+__host__ __device__ constexpr size_t means_buf_floats(int kmax) {
+  return (((size_t)kBMTile * (D + 4) + (size_t)kBMTile * (((kmax + 3) & ~3) + 1)) + 3) & ~(size_t)3;
+}
+
 template <int D>
 __global__ void __launch_bounds__(kBMThreads)
 k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const MItem *__restrict__ items,
-          double *__restrict__ mpart) {
-  constexpr int XC = D + 4, NQB = XC / 4, SR = kBMaxK + 1, TP = kBMTile;
+          double *__restrict__ mpart, int kmax) {
+  constexpr int XC = D + 4, NQB = XC / 4, TP = kBMTile;
   constexpr int UPT = (kBMaxK / 4 * NQB + kBMThreads - 1) / kBMThreads;
-  constexpr int XPT = (TP * XC + kBMThreads - 1) / kBMThreads;
-  constexpr int RPT = (kBMaxK * TP + kBMThreads - 1) / kBMThreads;
-  static_assert(TP * SR >= kBMThreads * 16, "group reduction buffer");
-  __shared__ __align__(16) float sX[TP * XC];
-  __shared__ __align__(16) float sR[TP * SR];
+  extern __shared__ __align__(16) float msm[];
   const MItem item = items[blockIdx.x];
   if (!state[item.fit].active) return;
   const BFit &F = fits[item.fit];
@@ -341,7 +344,8 @@ k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const
   const float *__restrict__ R = F.R;
   const int64_t n = F.n;
   const int d = F.d, K = F.k, tid = threadIdx.x;
-  const int K4 = (K + 3) & ~3, nmt = (K4 / 4) * NQB;
+  const int K4 = (K + 3) & ~3, SR = ((kmax + 3) & ~3) + 1, nmt = (K4 / 4) * NQB;
+  const size_t bufsz = means_buf_floats<D>(kmax);
   const bool grouped = nmt <= kBMThreads;
   const int UG = grouped ? (nmt + 31) & ~31 : kBMThreads;
   const int MG = grouped ? kBMThreads / UG : 1;
@@ -350,23 +354,23 @@ k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const
   int mt[UPT];
 #pragma unroll
   for (int u = 0; u < UPT; u++) mt[u] = grouped ? (u == 0 ? tid % UG : nmt) : tid + u * kBMThreads;
-  float xr[XPT], rr[RPT];
-  auto fetch = [&](int t0) {
+  // columns d..D-1 and D+1..D+3 stay zero; posterior columns K..K4-1 too
+  for (size_t e = tid; e < 2 * bufsz; e += kBMThreads) msm[e] = 0.f;
+  __syncthreads();
+  auto stage = [&](int buf, int t0) {
+    float *sx = msm + buf * bufsz, *sr = sx + TP * XC;
     const int tp = min(TP, item.p1 - t0);
-#pragma unroll
-    for (int u = 0; u < XPT; u++) {
-      const int e = tid + u * kBMThreads, p = e / XC, c = e - p * XC;
-      float v = 0.f;
-      if (e < TP * XC && p < tp) v = c < d ? X[(size_t)(t0 + p) * d + c] : (c == D ? 1.f : 0.f);
-      xr[u] = v;
+    for (int e = tid; e < TP * d; e += kBMThreads) {
+      const int p = e / d, c = e - p * d;
+      cp_async4(sx + p * XC + c, X + (p < tp ? (size_t)(t0 + p) * d + c : 0), p < tp);
     }
-#pragma unroll
-    for (int u = 0; u < RPT; u++) {
-      const int e = tid + u * kBMThreads, j = e / TP, p = e - j * TP;
-      rr[u] = (j < K && p < tp) ? R[(size_t)j * n + t0 + p] : 0.f;
+    for (int e = tid; e < K * TP; e += kBMThreads) {
+      const int j = e / TP, p = e - j * TP;
+      cp_async4(sr + p * SR + j, R + (size_t)j * n + (p < tp ? t0 + p : 0), p < tp);
     }
+    for (int p = tid; p < TP; p += kBMThreads) sx[p * XC + D] = p < tp ? 1.f : 0.f;
+    cp_async_commit();
   };
-  fetch(item.p0);
   float acc[UPT][4][4];
 #pragma unroll
   for (int u = 0; u < UPT; u++)
@@ -374,28 +378,22 @@ k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const
     for (int a = 0; a < 4; a++)
 #pragma unroll
       for (int b = 0; b < 4; b++) acc[u][a][b] = 0.f;
-  for (int t0 = item.p0; t0 < item.p1; t0 += TP) {
+  stage(0, item.p0);
+  int buf = 0;
+  for (int t0 = item.p0; t0 < item.p1; t0 += TP, buf ^= 1) {
+    if (t0 + TP < item.p1) stage(buf ^ 1, t0 + TP);
+    else cp_async_commit();
+    cp_async_wait_prev();
     __syncthreads();
-#pragma unroll
-    for (int u = 0; u < XPT; u++) {
-      const int e = tid + u * kBMThreads;
-      if (e < TP * XC) sX[e] = xr[u];
-    }
-#pragma unroll
-    for (int u = 0; u < RPT; u++) {
-      const int e = tid + u * kBMThreads, j = e / TP, p = e - j * TP;
-      if (j < K4) sR[p * SR + j] = rr[u];
-    }
-    __syncthreads();
-    if (t0 + TP < item.p1) fetch(t0 + TP);
+    const float *sx = msm + buf * bufsz, *sr = sx + TP * XC;
     if (gok) {
 #pragma unroll
       for (int u = 0; u < UPT; u++) {
         if (mt[u] < nmt) {
           const int jb = mt[u] / NQB, qb = mt[u] - jb * NQB;
           for (int p = g; p < TP; p += MG) {
-            const float *rp = sR + p * SR + 4 * jb;
-            const float4 xv = *reinterpret_cast<const float4 *>(sX + p * XC + 4 * qb);
+            const float *rp = sr + p * SR + 4 * jb;
+            const float4 xv = *reinterpret_cast<const float4 *>(sx + p * XC + 4 * qb);
             const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
             for (int a = 0; a < 4; a++) {
@@ -407,11 +405,11 @@ k_b_means(const BFit *__restrict__ fits, const BState *__restrict__ state, const
         }
       }
     }
+    __syncthreads();
   }
   if (MG > 1) {
     // point groups 1.. hand their sums to group 0 (in group order)
-    float *red = sR;
-    __syncthreads();
+    float *red = msm;
     if (gok && g > 0 && mt[0] < nmt)
 #pragma unroll
       for (int a = 0; a < 4; a++)
@@ -940,6 +938,7 @@ struct fem_em_batch {
   int e_beg[kClasses + 1] = {}, m_beg[kClasses + 1] = {}, c_beg[kClasses + 1] = {};
   size_t c_smem[kClasses] = {};
   int c_kmax[kClasses] = {};       // largest k of the class's fits
+  size_t m_smem[kClasses] = {};     // means kernel dynamic shared memory
   std::vector<BState> hstate;
   // timing: phase boundaries of the sweeps since the last host sync
   bool timing = false;
@@ -1061,10 +1060,10 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     }
     const MItem *it0 = b->mitems + b->m_beg[c];
     switch (c) {
-      case 0: k_b_means<4><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
-      case 1: k_b_means<8><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
-      case 2: k_b_means<16><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
-      default: k_b_means<32><<<cnt, kBMThreads, 0, b->stream>>>(fits, st, it0, b->mpart); break;
+      case 0: k_b_means<4><<<cnt, kBMThreads, b->m_smem[c], b->stream>>>(fits, st, it0, b->mpart, b->c_kmax[c]); break;
+      case 1: k_b_means<8><<<cnt, kBMThreads, b->m_smem[c], b->stream>>>(fits, st, it0, b->mpart, b->c_kmax[c]); break;
+      case 2: k_b_means<16><<<cnt, kBMThreads, b->m_smem[c], b->stream>>>(fits, st, it0, b->mpart, b->c_kmax[c]); break;
+      default: k_b_means<32><<<cnt, kBMThreads, b->m_smem[c], b->stream>>>(fits, st, it0, b->mpart, b->c_kmax[c]); break;
     }
     FEM_CUDA(cudaGetLastError());
     b->launches++;
@@ -1245,6 +1244,17 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
     const int D = class_dim(c), nblk = class_nblk(D);
     const int cj = std::max(1, std::min(kmax, 256 / nblk + 2));
     b->c_kmax[c] = std::max(kmax, 1);
+    {
+      size_t mf = 0;
+      switch (c) {
+        case 0: mf = means_buf_floats<4>(b->c_kmax[c]); break;
+        case 1: mf = means_buf_floats<8>(b->c_kmax[c]); break;
+        case 2: mf = means_buf_floats<16>(b->c_kmax[c]); break;
+        default: mf = means_buf_floats<32>(b->c_kmax[c]); break;
+      }
+      // two tile buffers; the point-group reduction reuses them (<= 128 x 16 floats)
+      b->m_smem[c] = std::max<size_t>(2 * mf, (size_t)kBMThreads * 16) * sizeof(float);
+    }
     b->c_smem[c] = (class_owner(D) ? 2 * own_buf_floats(D, b->c_kmax[c]) : CovGeom<32>::floats(cj)) * sizeof(float);
   }
   b->e_beg[kClasses] = (int)ei.size();
@@ -1275,6 +1285,10 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
       allow_dyn_smem(k_b_estep<8, kBEP>, estep_smem<8>()) != cudaSuccess ||
       allow_dyn_smem(k_b_estep<16, kBEP>, estep_smem<16>()) != cudaSuccess ||
       allow_dyn_smem(k_b_estep<32, kBEP>, estep_smem<32>()) != cudaSuccess ||
+      allow_dyn_smem(k_b_means<4>, b->m_smem[0]) != cudaSuccess ||
+      allow_dyn_smem(k_b_means<8>, b->m_smem[1]) != cudaSuccess ||
+      allow_dyn_smem(k_b_means<16>, b->m_smem[2]) != cudaSuccess ||
+      allow_dyn_smem(k_b_means<32>, b->m_smem[3]) != cudaSuccess ||
       allow_dyn_smem(k_b_cov_own<4>, b->c_smem[0]) != cudaSuccess ||
       allow_dyn_smem(k_b_cov_own<8>, b->c_smem[1]) != cudaSuccess ||
       allow_dyn_smem(k_b_cov_own<16>, b->c_smem[2]) != cudaSuccess ||

@@ -146,3 +146,21 @@ def test_batch_rejects_unsupported_shapes(gpu_lib):
     for shape in [(33, 1000, 4), (8, 1000, 65)]:
         with pytest.raises(C.FemError, match="batched fits need"):
             CudaBatchEM([(4, 1000, 2), shape])
+
+
+def test_batch_edge_shapes(gpu_lib, oracle):
+    """d = 1, K = 1, fits smaller than one E-step item (512 points) or just
+    over it, n barely above d, 64 components in 2 dimensions: each fit's
+    trace against the FP64 oracle."""
+    shapes = [(1, 500, 1, 701), (1, 1000, 3, 702), (3, 40, 2, 703), (32, 200, 1, 704), (7, 513, 2, 705),
+              (2, 5000, 64, 706)]
+    data = []
+    for d, n, k, seed in shapes:
+        X, _ = synth.kmeans_blobs(seed=seed, n=n, d=d, k=k, spread=6.0)
+        data.append((X, synth.dsquared_init(X, k, seed=seed - 700)))
+    got = train_batch(data, 6)
+    for i, (X, init) in enumerate(data):
+        ref = oracle.em_train(X, *init, 6, eps=0.0, abort_thr=1e12)
+        assert ref["status"] == 0 and got["status"][i] == 0 and got["iters"][i] == ref["iter_counter"]
+        err = np.max(np.abs(got["traces"][i][0] - ref["logl"])) / len(X)
+        assert err <= 1e-5, (shapes[i], err)
