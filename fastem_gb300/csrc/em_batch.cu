@@ -832,8 +832,8 @@ k_b_factor(const BFit *__restrict__ fits, BState *__restrict__ state, const int2
     return;
   }
   block_lower_inverse(sA, d, sWi);
+  const double ld = block_chol_logdet(sA, d);
   if (tid == 0) {
-    const double ld = chol_logdet(sA, d);
     const double lc = log(F.pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
     F.logc[j] = lc;
     F.logcT[j] = (float)lc;

@@ -71,25 +71,44 @@ __device__ inline bool block_cholesky(const double *S, int d, double *A) {
   return ok;
 }
 
+constexpr int kFactorMaxD = 256;   // largest d of the block factorisation helpers
+
 // W = L^-1 (lower, row-major) by forward substitution, threads owning columns;
-// L is the lower triangle of A
+// L is the lower triangle of A.  The diagonal's reciprocals are formed once,
+// in parallel, so a column's substitution multiplies instead of dividing.
+// d <= kFactorMaxD.
 __device__ inline void block_lower_inverse(const double *A, int d, double *Wi) {
+  __shared__ double s_rd[kFactorMaxD];
+  for (int r = threadIdx.x; r < d; r += blockDim.x) s_rd[r] = 1.0 / A[(size_t)r * d + r];
+  __syncthreads();
   for (int c = threadIdx.x; c < d; c += blockDim.x) {
     for (int r = 0; r < c; r++) Wi[(size_t)r * d + c] = 0.0;
     for (int r = c; r < d; r++) {
       double s = (r == c) ? 1.0 : 0.0;
       for (int m2 = c; m2 < r; m2++) s -= A[(size_t)r * d + m2] * Wi[(size_t)m2 * d + c];
-      Wi[(size_t)r * d + c] = s / A[(size_t)r * d + r];
+      Wi[(size_t)r * d + c] = s * s_rd[r];
     }
   }
   __syncthreads();
 }
 
-// log det = 2 sum log L_ii (L in the lower triangle of A), summed in order
-__device__ inline double chol_logdet(const double *A, int d) {
-  double ld = 0.0;
-  for (int q = 0; q < d; q++) ld += log(A[(size_t)q * d + q]);
-  return 2.0 * ld;
+// log det = 2 sum log L_ii (L in the lower triangle of A): the logarithms in
+// parallel, summed in index order by one thread; the value in every thread.
+// d <= kFactorMaxD.
+__device__ inline double block_chol_logdet(const double *A, int d) {
+  __shared__ double s_log[kFactorMaxD];
+  __shared__ double s_ld;
+  for (int q = threadIdx.x; q < d; q += blockDim.x) s_log[q] = log(A[(size_t)q * d + q]);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ld = 0.0;
+    for (int q = 0; q < d; q++) ld += s_log[q];
+    s_ld = 2.0 * ld;
+  }
+  __syncthreads();
+  const double v = s_ld;
+  __syncthreads();
+  return v;
 }
 
 // NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71): the

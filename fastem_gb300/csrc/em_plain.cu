@@ -425,8 +425,8 @@ k_factor(int K, int d, double reg, int regularize, double *__restrict__ sigma,
     return;
   }
   block_lower_inverse(A, d, Wi);
+  const double ld = block_chol_logdet(A, d);
   if (tid == 0) {
-    const double ld = chol_logdet(A, d);
     logdet[j] = ld;
     const double lc = log(pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
     logc[j] = lc;
