@@ -41,7 +41,8 @@ EXPORTS = [
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_correct_without_mse",
-    "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_stats",
+    "fem_km_run", "fem_km_get_assignment", "fem_km_seed", "fem_km_set_rng_state", "fem_km_get_rng_state",
+    "fem_km_stats",
     "fem_km_classify_noalloc",
 ]
 
@@ -133,6 +134,8 @@ def lib():
         "fem_km_run": ([P, P, f64, i32, P, P], i32),
         "fem_km_get_assignment": ([P, P], i32),
         "fem_km_seed": ([P, ctypes.c_uint64], i32),
+        "fem_km_set_rng_state": ([P, ctypes.c_char_p], i32),
+        "fem_km_get_rng_state": ([P, ctypes.c_char_p, ctypes.c_size_t], i32),
         "fem_km_stats": ([P, P, P, P], i32),
         "fem_km_classify_noalloc": ([i32, i64, i32, P, P, P, P, i32, P], i32),
     }

@@ -6,6 +6,7 @@
                      GaussianMixture / KMeansAlgorithm interfaces on top of
                      the C-ABI, plus the .bin / .cmp formats.
   em2gpu             command-line driver mirroring the reference's em2.
+  eminitgpu          command-line driver mirroring the reference's eminit.
 
 Translation units compile in parallel; a unit is rebuilt when it or any
 header is newer than its object file.
@@ -25,6 +26,8 @@ OBJ = os.path.join(HERE, "_build")
 GPU_LIB = os.path.join(HERE, "libfastem_gpu.so")
 HOST_LIB = os.path.join(HERE, "libfastem_host.so")
 EM2GPU = os.path.join(HERE, "em2gpu")
+EMINITGPU = os.path.join(HERE, "eminitgpu")
+DRIVERS = {"em2gpu.cpp": EM2GPU, "eminitgpu.cpp": EMINITGPU}   # source -> program
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -105,18 +108,19 @@ def build_host(verbose=False):
     if not srcs:
         return None
     hdrs = glob.glob(os.path.join(HOST, "*.h")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
-    lib_srcs = [s for s in srcs if not s.endswith("em2gpu.cpp")]
+    lib_srcs = [s for s in srcs if os.path.basename(s) not in DRIVERS]
     cxx = os.environ.get("CXX", "g++")
-    _drop_foreign([HOST_LIB, EM2GPU])
+    _drop_foreign([HOST_LIB] + list(DRIVERS.values()))
     common = ["-O2", "-std=c++17", "-fPIC", "-I" + os.path.join(ROOT, "include"), "-I" + HOST]
     newest = _newest(srcs + hdrs + [GPU_LIB])
     if not os.path.exists(HOST_LIB) or os.path.getmtime(HOST_LIB) < newest:
         _run([cxx] + common + ["-shared", "-o", HOST_LIB] + lib_srcs +
              ["-L" + HERE, "-lfastem_gpu", "-Wl,-rpath,$ORIGIN"], verbose)
-    drv = os.path.join(HOST, "em2gpu.cpp")
-    if os.path.exists(drv) and (not os.path.exists(EM2GPU) or os.path.getmtime(EM2GPU) < newest):
-        _run([cxx] + common + ["-o", EM2GPU, drv, "-L" + HERE, "-lfastem_host", "-lfastem_gpu",
-                               "-Wl,-rpath,$ORIGIN"], verbose)
+    for src, exe in DRIVERS.items():
+        drv = os.path.join(HOST, src)
+        if os.path.exists(drv) and (not os.path.exists(exe) or os.path.getmtime(exe) < newest):
+            _run([cxx] + common + ["-o", exe, drv, "-L" + HERE, "-lfastem_host", "-lfastem_gpu",
+                                   "-Wl,-rpath,$ORIGIN"], verbose)
     return HOST_LIB
 
 

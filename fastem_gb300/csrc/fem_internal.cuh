@@ -150,6 +150,7 @@ struct fem_km {
   bool have_data = false;
   std::mt19937_64 rng;
   std::uniform_real_distribution<> uni;
+  int64_t next_repair = 0;         // next row of FEM_KM_REPAIR_NEXT
 
   float *X = nullptr;              // n x d
   __nv_bfloat16 *Xb = nullptr;     // n x d (mixed)

@@ -16,7 +16,10 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <cstring>
 #include <new>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include "fem_internal.cuh"
@@ -397,7 +400,7 @@ void fem_km_config_default(fem_km_config *cfg) {
   cfg->precision = FEM_PREC_MIXED;
   cfg->device = 0;
   cfg->seed = 0;
-  cfg->repair = 1;
+  cfg->repair = FEM_KM_REPAIR_RANDOM;
 }
 
 int fem_km_create(int d, int64_t n, int k, const fem_km_config *cfg, fem_km **out) {
@@ -417,6 +420,10 @@ int fem_km_create(int d, int64_t n, int k, const fem_km_config *cfg, fem_km **ou
   }
   if (c.precision != FEM_PREC_FP32 && c.precision != FEM_PREC_MIXED) {
     set_error("k-means precision must be FEM_PREC_FP32 or FEM_PREC_MIXED");
+    return FEM_ERR_BAD_ARG;
+  }
+  if (c.repair != FEM_KM_REPAIR_NONE && c.repair != FEM_KM_REPAIR_RANDOM && c.repair != FEM_KM_REPAIR_NEXT) {
+    set_error("repair must be FEM_KM_REPAIR_NONE, FEM_KM_REPAIR_RANDOM or FEM_KM_REPAIR_NEXT");
     return FEM_ERR_BAD_ARG;
   }
   if (c.precision == FEM_PREC_FP32 && !(d == 2 || d == 4 || d == 8 || d == 16 || d == 32 || d == 64)) {
@@ -492,6 +499,32 @@ int fem_km_seed(fem_km *h, uint64_t seed) {
   return FEM_OK;
 }
 
+int fem_km_set_rng_state(fem_km *h, const char *state) {
+  FEM_TRY(check(h));
+  std::mt19937_64 r;
+  std::istringstream in(state ? state : "");
+  if (!state || !(in >> r)) {
+    set_error("fem_km_set_rng_state: not an mt19937_64 state");
+    return FEM_ERR_BAD_ARG;
+  }
+  h->rng = r;
+  h->uni.reset();
+  return FEM_OK;
+}
+
+int fem_km_get_rng_state(fem_km *h, char *buf, size_t len) {
+  FEM_TRY(check(h));
+  std::ostringstream out;
+  out << h->rng;
+  const std::string t = out.str();
+  if (!buf || len < t.size() + 1) {
+    set_error("fem_km_get_rng_state: %zu bytes needed", t.size() + 1);
+    return FEM_ERR_BAD_ARG;
+  }
+  std::memcpy(buf, t.c_str(), t.size() + 1);
+  return FEM_OK;
+}
+
 // one Lloyd iteration (NaiveKMA::ComputeMSEAndCorrect / CorrectWithoutMSE,
 // Clust/KMAlgorithm.cpp:148-255): labels, fixed-point sums, divide or repair;
 // with `changed` the kernels also report whether any label moved
@@ -542,8 +575,14 @@ static int km_iterate(fem_km *h, double *centroids, double *fit, int64_t *counts
     if (counts) counts[j] = nj;
     if (nj > 0) {
       for (int q = 0; q < d; q++) centroids[(size_t)j * d + q] = h->hout[(size_t)j * d + q];
-    } else if (h->cfg.repair) {
-      const int64_t src = (int64_t)(h->uni(h->rng) * (double)h->n);
+    } else if (h->cfg.repair != FEM_KM_REPAIR_NONE) {
+      int64_t src;
+      if (h->cfg.repair == FEM_KM_REPAIR_RANDOM) {
+        src = (int64_t)(h->uni(h->rng) * (double)h->n);
+      } else {
+        src = h->next_repair;
+        if (++h->next_repair == h->n) h->next_repair = 0;
+      }
       std::vector<float> row(d);
       FEM_CUDA(cudaMemcpy(row.data(), h->X + src * d, d * 4, cudaMemcpyDeviceToHost));
       for (int q = 0; q < d; q++) centroids[(size_t)j * d + q] = (double)row[q];

@@ -5,6 +5,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <sstream>
 #include <thread>
 
 namespace fastem {
@@ -237,6 +238,73 @@ int GaussianMixture::Classify(const float *x) const {
   return cls;
 }
 
+namespace {
+
+// |lambda_max / lambda_min| of the symmetric matrix whose lower triangle is
+// S (d x d, row-major): cyclic Jacobi rotations (the classical symmetric
+// Schur rotation, tangent of the smaller angle) until the off-diagonal mass
+// is below 1e-30 of the diagonal's, or 100 sweeps
+double condition_number(const double *S, int d) {
+  std::vector<double> A((size_t)d * d);
+  for (int r = 0; r < d; r++)
+    for (int c = 0; c < d; c++) A[(size_t)r * d + c] = c <= r ? S[(size_t)r * d + c] : S[(size_t)c * d + r];
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, dg = 0.0;
+    for (int r = 0; r < d; r++)
+      for (int c = 0; c < d; c++) {
+        const double v = A[(size_t)r * d + c];
+        if (c > r) off += v * v;
+        else if (c == r) dg += v * v;
+      }
+    if (!(off > 1e-30 * dg)) break;
+    for (int p = 0; p < d - 1; p++)
+      for (int q = p + 1; q < d; q++) {
+        const double apq = A[(size_t)p * d + q];
+        if (apq == 0.0) continue;
+        const double th = (A[(size_t)q * d + q] - A[(size_t)p * d + p]) / (2.0 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int r = 0; r < d; r++) {   // columns p, q
+          const double arp = A[(size_t)r * d + p], arq = A[(size_t)r * d + q];
+          A[(size_t)r * d + p] = cs * arp - sn * arq;
+          A[(size_t)r * d + q] = sn * arp + cs * arq;
+        }
+        for (int r = 0; r < d; r++) {   // rows p, q
+          const double apr = A[(size_t)p * d + r], aqr = A[(size_t)q * d + r];
+          A[(size_t)p * d + r] = cs * apr - sn * aqr;
+          A[(size_t)q * d + r] = sn * apr + cs * aqr;
+        }
+      }
+  }
+  double mn = A[0], mx = A[0];
+  for (int p = 1; p < d; p++) mn = std::min(mn, A[(size_t)p * d + p]), mx = std::max(mx, A[(size_t)p * d + p]);
+  return std::fabs(mx / mn);
+}
+
+}  // namespace
+
+double GaussianMixture::FindLargestConditionNumber() const {
+  double maxcond = 1.0;
+  for (int j = 0; j < K; j++) maxcond = std::max(maxcond, condition_number(GetCovariance(j), d));
+  return maxcond;
+}
+
+void GaussianMixture::Dump(FILE *f) const {
+  std::fprintf(f, "Number of components: %d\n", K);
+  for (int j = 0; j < K; j++) {
+    std::fprintf(f, "Component %d: \n", j);
+    std::fprintf(f, "Mixing probability: %g\n", weights[j]);
+    std::fprintf(f, "Mean vector: ");
+    for (int q = 0; q < d; q++) std::fprintf(f, "%.3g ", GetMean(j)[q]);
+    std::fprintf(f, "\nCovariance matrix\n");
+    for (int a = 0; a < d; a++) {
+      for (int b = 0; b < d; b++) std::fprintf(f, "%.3g ", GetCovariance(j)[(size_t)a * d + b]);
+      std::fprintf(f, "\n");
+    }
+  }
+  std::fprintf(f, "Condition number of the solution: %g\n", FindLargestConditionNumber());
+}
+
 // ---------------------------------------------------------------------- EM
 CudaEM::CudaEM(int ncols, int64_t nrows, int ncl, int precision, int device) : nCols(ncols), K(ncl), nRows(nrows) {
   fem_em_config cfg;
@@ -331,6 +399,37 @@ void CudaKMeans::InitDataStructures() { check(fem_km_init_data_structures(h)); }
 void CudaKMeans::Assignment(std::vector<int32_t> &labels) const {
   labels.resize(nRows);
   check(fem_km_get_assignment(h, labels.data()));
+}
+
+void CudaKMeans::SetRngState(const std::string &state) { check(fem_km_set_rng_state(h, state.c_str())); }
+
+std::string CudaKMeans::GetRngState() const {
+  std::vector<char> buf(FEM_KM_RNG_STATE_LEN);
+  check(fem_km_get_rng_state(h, buf.data(), buf.size()));
+  return std::string(buf.data());
+}
+
+std::string Rand::State() const {
+  std::ostringstream out;
+  out << rng;
+  return out.str();
+}
+
+void Rand::SetState(const std::string &state) {
+  std::istringstream in(state);
+  if (!(in >> rng)) throw std::invalid_argument("not an mt19937_64 state");
+  uni.reset();
+}
+
+std::vector<double> Forgy(const Dataset &data, int K, Rand &rnd) {
+  const int64_t N = data.GetRowCount();
+  const int d = data.GetColCount();
+  std::vector<double> C((size_t)K * d);
+  for (int j = 0; j < K; j++) {
+    const int64_t obj = (int64_t)(rnd() * (double)N);
+    for (int q = 0; q < d; q++) C[(size_t)j * d + q] = data.GetRow(obj)[q];
+  }
+  return C;
 }
 
 // ------------------------------------------------------------ initialisers
@@ -436,7 +535,7 @@ namespace {
 // KMeansEMInitializer::Init after the seeding (EM2/EMInitializer.cpp:103-134):
 // 30 k-means iterations with MinRel 1e-4 on the GPU, the classes of the final
 // centroids, then the class covariances (divided by count - 1) and weights
-GaussianMixture MixtureFromCentroids(const Dataset &data, std::vector<double> C, int K, int precision,
+GaussianMixture MixtureFromCentroids(const Dataset &data, std::vector<double> C, int K, Rand &rnd, int precision,
                                      int device) {
   const int64_t N = data.GetRowCount();
   const int d = data.GetColCount();
@@ -444,7 +543,9 @@ GaussianMixture MixtureFromCentroids(const Dataset &data, std::vector<double> C,
   {
     const int kprec = (precision == FEM_PREC_MIXED && d == 32) ? FEM_PREC_MIXED : FEM_PREC_FP32;
     CudaKMeans km(data, K, kprec, device, 0, true);
+    km.SetRngState(rnd.State());   // CentroidRandomRepair draws from the same Rand() stream
     km.RunKMeans(C, 0, 1e-4, 30);
+    rnd.SetState(km.GetRngState());
     // the classes of the final centroids (ClassifyDataset): one more assignment
     std::vector<double> C2 = C;
     km.ComputeMSEAndCorrect(C2);
@@ -485,16 +586,22 @@ GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &
   const int64_t N = data.GetRowCount();
   const int d = data.GetColCount();
   if (name == nullptr || !std::strcmp(name, "jain")) {
-    // JainEMInitializer: distinct random rows as means, tr(Cov)/d/10 I, 1/K
+    // JainEMInitializer::Init (EM2/EMInitializer.cpp:43-77): means are rows
+    // at Rand() * N, covariances tr(Cov) / d / 10 I, weights 1 / K.  The
+    // reference draws a component's row once, then keeps drawing until a
+    // draw misses the rows already taken, but keeps the first draw (the
+    // repeat test reads a shadowing variable): the same rows and the same
+    // use of the stream here, repeats included.
     GaussianMixture G(K, d);
     const double cv = data.GetCovMatrixTrace() / d / 10.0;
-    std::vector<int64_t> used;
+    std::vector<int64_t> taken;
     for (int j = 0; j < K; j++) {
-      int64_t idx;
-      do {
-        idx = std::min<int64_t>(N - 1, (int64_t)(rnd() * (double)N));
-      } while (std::find(used.begin(), used.end(), idx) != used.end() && (int64_t)used.size() < N);
-      used.push_back(idx);
+      const int64_t idx = (int64_t)(rnd() * (double)N);
+      for (;;) {
+        const int64_t again = (int64_t)(rnd() * (double)N);
+        if (std::find(taken.begin(), taken.end(), again) == taken.end()) break;
+      }
+      taken.push_back(idx);
       for (int q = 0; q < d; q++) G.Means()[(size_t)j * d + q] = data.GetRow(idx)[q];
       for (int a = 0; a < d; a++)
         for (int b = 0; b < d; b++) G.Covs()[((size_t)j * d + a) * d + b] = a == b ? cv : 0.0;
@@ -503,14 +610,14 @@ GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &
     return G;
   }
   if (!std::strcmp(name, "kmeans")) {
-    // KMeansEMInitializer: k-means++ centroids (D^2 sampling over at most
-    // 2^18 evenly spread rows), then k-means and class covariances
-    return MixtureFromCentroids(data, KMeansPlusPlus(data, K, rnd, 1 << 18), K, precision, device);
+    // KMeansEMInitializer (EM2/EMInitializer.cpp:80-134): Forgy centroids,
+    // then k-means and class covariances
+    return MixtureFromCentroids(data, Forgy(data, K, rnd), K, rnd, precision, device);
   }
   if (!std::strcmp(name, "kmeansoror")) {
     // KMeansOrOrEMInitializer (EM2/EMInitializer.cpp:153-157): k-means||
     // centroids with oversampling 1.4, then as above
-    return MixtureFromCentroids(data, KMeansOrOr(data, K, rnd, 1.4), K, precision, device);
+    return MixtureFromCentroids(data, KMeansOrOr(data, K, rnd, 1.4), K, rnd, precision, device);
   }
   return GaussianMixture::Read(name);
 }

@@ -87,6 +87,15 @@ class GaussianMixture {
   double Evaluate(const float *x) const;
   int Classify(const float *x) const;
 
+  // largest lambda_max / lambda_min over the components' covariances
+  // (GaussianMixture::FindLargestConditionNumber, EM2/GaussianMixture.cpp;
+  // NormalDensity::ComputeConditionNumber, EM2/NormalDensity.cpp:67-71):
+  // eigenvalues by cyclic Jacobi in FP64 on the host
+  double FindLargestConditionNumber() const;
+  // the components' weights, means and covariances, then the condition
+  // number, as GaussianMixture::Dump (EM2/GaussianMixture.cpp:139-153) prints them
+  void Dump(FILE *f = stdout) const;
+
  private:
   void Factor() const;
   double LogDensities(const float *x, std::vector<double> &l) const;
@@ -139,6 +148,10 @@ class CudaKMeans {
   void InitDataStructures();
   int GetIterCount() const { return iterCount; }
   void Assignment(std::vector<int32_t> &labels) const;
+  // repairs continue the caller's Rand() stream (the reference's one global
+  // generator): copy its state in before and back out after the iterations
+  void SetRngState(const std::string &state);
+  std::string GetRngState() const;
 
  private:
   fem_km *h = nullptr;
@@ -153,12 +166,18 @@ class Rand {
  public:
   explicit Rand(uint64_t seed) : rng(seed) {}
   double operator()() { return uni(rng); }
+  // the generator's state as the standard library's stream operators write it
+  std::string State() const;
+  void SetState(const std::string &state);
 
  private:
   std::mt19937_64 rng;
   std::uniform_real_distribution<> uni;
 };
 
+// Forgy centroids (ForgyInitializer::Init, Clust/KMeansInitializer.cpp:33-49):
+// K rows at Rand() * N, repeats allowed
+std::vector<double> Forgy(const Dataset &data, int K, Rand &rnd);
 // k-means++ centroids (Clust/PlusPlusInitializer/PlusPlusInitializer.cpp:33-83),
 // FP64 on the host over `sample` rows spread evenly over the dataset (all rows,
 // as the reference, if sample <= 0 or >= N)

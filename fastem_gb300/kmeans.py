@@ -20,7 +20,9 @@ class CudaKMA:
         cfg.precision = C.PREC[precision]
         cfg.device = device
         cfg.seed = int(seed)
-        cfg.repair = int(bool(repair))
+        # True / "random": CentroidRandomRepair; "next": CentroidDeterministicRepair;
+        # False / "none": empty clusters keep their centroid
+        cfg.repair = {False: 0, True: 1, "none": 0, "random": 1, "next": 2}[repair]
         h = ctypes.c_void_p()
         C.check(C.lib().fem_km_create(int(ncols), int(nrows), int(nclusters), ctypes.byref(cfg),
                                       ctypes.byref(h)))

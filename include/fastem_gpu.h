@@ -25,6 +25,7 @@
 #ifndef FASTEM_GPU_H_
 #define FASTEM_GPU_H_
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -194,11 +195,16 @@ int fem_em_batch_timing_classes(fem_em_batch *b, double *class_ms);
 
 typedef struct fem_km fem_km;
 
+enum { FEM_KM_REPAIR_NONE = 0, FEM_KM_REPAIR_RANDOM = 1, FEM_KM_REPAIR_NEXT = 2 };
+
 typedef struct fem_km_config {
   int precision;   /* FEM_PREC_FP32 (CUDA-core distances) or FEM_PREC_MIXED (tcgen05, FP16 hi/lo splits) */
   int device;
   uint64_t seed;   /* seed of the repair RNG (Util/Rand.cpp SRand) */
-  int repair;      /* 1: CentroidRandomRepair (Clust/CentroidRepair.cpp:21-28); 0: leave empty */
+  int repair;      /* an empty cluster's centroid becomes: FEM_KM_REPAIR_RANDOM the row at Rand() * N
+                      (CentroidRandomRepair, Clust/CentroidRepair.cpp:21-28); FEM_KM_REPAIR_NEXT rows
+                      0, 1, 2, ... in turn, wrapping at N, one counter per handle
+                      (CentroidDeterministicRepair, :30-43); FEM_KM_REPAIR_NONE unchanged */
 } fem_km_config;
 
 void fem_km_config_default(fem_km_config *cfg);
@@ -229,6 +235,16 @@ int fem_km_run(fem_km *h, double *centroids, double min_rel, int max_iter, doubl
 int fem_km_get_assignment(fem_km *h, int32_t *labels);
 /* reseed the repair RNG (SRand, Util/Rand.cpp:33-35) */
 int fem_km_seed(fem_km *h, uint64_t seed);
+/* The reference repairs empty clusters from its one global Rand() stream
+ * (Util/Rand.cpp:7-14, Clust/CentroidRepair.cpp:21-28), which the seeding
+ * drew from first.  These copy the repair RNG's std::mt19937_64 state in and
+ * out as the text the C++ standard library's stream operators write, so a
+ * host that seeds with its own generator continues the same stream.
+ * fem_km_get_rng_state needs len > the text's length (about 7 KB;
+ * FEM_KM_RNG_STATE_LEN is enough). */
+#define FEM_KM_RNG_STATE_LEN 8192
+int fem_km_set_rng_state(fem_km *h, const char *state);
+int fem_km_get_rng_state(fem_km *h, char *buf, size_t len);
 
 /* k-means classification that allocates nothing.  No counterpart in the
  * reference: a handle-free variant of the assignment kernel with the

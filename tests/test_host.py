@@ -164,3 +164,95 @@ def test_em2gpu_accepts_reference_cpu_options(em2gpu):
     # well-formed options get as far as opening the (missing) data file
     ok = run("-N", "automax:32", "-A", "simplematrixem", "-R", "log2", "-M", "simple", "missing.bin")
     assert ok.returncode != 0 and "MStepLoopParam" not in ok.stderr and "algorithm" not in ok.stderr
+
+
+@pytest.fixture(scope="module")
+def eminit(em2gpu):
+    from fastem_gb300 import build
+    assert os.path.exists(build.EMINITGPU)
+    return build.EMINITGPU
+
+
+def jain_rows(n, k, seed, oracle):
+    """JainEMInitializer::Init's draws (EM2/EMInitializer.cpp:43-77) from the
+    oracle's Rand(): a component keeps its first draw; further draws repeat
+    until one misses the rows already taken."""
+    oracle.rng_seed(seed)
+    taken = []
+    for _ in range(k):
+        idx = int(oracle.rng_uniform() * n)
+        while int(oracle.rng_uniform() * n) in taken:
+            pass
+        taken.append(idx)
+    return taken
+
+
+def test_eminit_jain(eminit, oracle, tmp_path):
+    """eminitgpu -I jain: the reference's rows (a repeated row included, as
+    its repeat test reads a shadowing variable), tr(Cov) / d / 10 I, 1 / K."""
+    X, _ = synth.kmeans_blobs(seed=5, n=60, d=3, k=4)
+    fb, fo = str(tmp_path / "j.bin"), str(tmp_path / "j.cmp")
+    formats.write_bin(fb, X)
+    out = subprocess.run([eminit, "-I", "jain", "-c", "7", "-r", "11", "-o", fo, fb], capture_output=True,
+                         text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    G, _ = formats.read_cmp(fo)
+    rows = jain_rows(len(X), 7, 11, oracle)
+    assert len(set(rows)) < len(rows)          # this seed repeats a row
+    np.testing.assert_array_equal(G.means, X[rows].astype(np.float64))
+    cv = np.trace(np.cov(X.astype(np.float64).T)) / 3 / 10
+    np.testing.assert_allclose(G.covs, np.broadcast_to(np.eye(3) * cv, (7, 3, 3)), rtol=1e-12)
+    np.testing.assert_array_equal(G.weights, np.full(7, 1.0 / 7))
+
+
+def test_eminit_file_dump_and_arguments(eminit, tmp_path):
+    """-I file.cmp without -o prints the mixture as GaussianMixture::Dump,
+    ending with the largest condition number; bad options are refused as
+    eminit's ProcessArgs refuses them."""
+    z = np.load(os.path.join(GOLDEN, "em_small.npz"))
+    fb, fi = str(tmp_path / "x.bin"), str(tmp_path / "g.cmp")
+    formats.write_bin(fb, z["X"])
+    formats.write_cmp(fi, GaussianMixture(z["pi"], z["mu"], z["sigma"]))
+    out = subprocess.run([eminit, "-I", fi, "-c", "3", fb], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "File EM initializer" in out.stdout and out.stdout.count("Covariance matrix\n") == 3
+    cond = float(out.stdout.split("Condition number of the solution:")[1].split()[0])
+    ev = [np.linalg.eigvalsh(s) for s in z["sigma"]]
+    assert cond == pytest.approx(max(abs(e[-1] / e[0]) for e in ev), rel=1e-5)   # printed with %g
+    for args, msg in [(["-c", "0", fb], "invalid value of -c option"), (["-r", "-2", fb], "invalid value of -r option"),
+                      (["-c", "2"], "Missing dataset name")]:
+        bad = subprocess.run([eminit] + args, capture_output=True, text=True, timeout=60)
+        assert bad.returncode == 1 and "Invalid program argument: " + msg in bad.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,d,k,data_seed", [(5000, 8, 6, 3), (200, 4, 12, 4)])
+def test_eminit_kmeans_matches_oracle(eminit, oracle, tmp_path, n, d, k, data_seed):
+    """eminitgpu -I kmeans = KMeansEMInitializer::Init (EM2/EMInitializer.cpp:
+    103-134): Forgy rows, RunKMeans(0, 1e-4, 30) with empty clusters repaired
+    from the same Rand() stream, the classes of the final centroids, class
+    covariances / (count - 1), weights count / N.  The second shape takes a
+    seed whose Forgy rows repeat, so a repair draws from the stream."""
+    X, _ = synth.kmeans_blobs(seed=data_seed, n=n, d=d, k=max(2, k // 2), spread=6.0)
+    seed = 0
+    while True:
+        oracle.rng_seed(seed)
+        rows = [int(oracle.rng_uniform() * n) for _ in range(k)]
+        if (len(set(rows)) < k) == (n < 1000):
+            break
+        seed += 1
+    fb, fo = str(tmp_path / "x.bin"), str(tmp_path / "g.cmp")
+    formats.write_bin(fb, X)
+    out = subprocess.run([eminit, "-I", "kmeans", "-c", str(k), "-r", str(seed), "-p", "fp32", "-o", fo, fb],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    G, _ = formats.read_cmp(fo)
+    C = oracle.kmeans_forgy(X, k, seed=seed)
+    _, C, _ = oracle.km_run(X, C, min_rel=1e-4, max_iter=30)
+    _, _, counts, labels = oracle.km_iterate(X, C, repair=False)
+    np.testing.assert_allclose(G.means, C, rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(G.weights, counts / n)
+    X64 = X.astype(np.float64)
+    for j in range(k):
+        R = X64[labels == j] - C[j]
+        np.testing.assert_allclose(G.covs[j], R.T @ R / (counts[j] - 1.0), rtol=1e-9, atol=1e-12)

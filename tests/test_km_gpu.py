@@ -79,6 +79,27 @@ def test_km_empty_cluster_repair(gpu_lib, oracle):
     check_iters(out)
 
 
+def test_km_deterministic_repair(gpu_lib, oracle):
+    """repair="next" (CentroidDeterministicRepair, Clust/CentroidRepair.cpp:
+    30-43): empty clusters take rows 0, 1, 2, ... in index order, the counter
+    carried from one iteration to the next; the other centroids as without
+    repair."""
+    X, _ = synth.kmeans_blobs(seed=6, n=1000, d=4, k=3)
+    C0 = np.vstack([X[:3].astype(np.float64), np.full((2, 4), 1e6)])
+    with CudaKMA(4, len(X), 5, precision="fp32", repair="next") as km:
+        km.SetDataset(X)
+        C = C0.copy()
+        _, counts = km.ComputeMSEAndCorrectCounts(C)
+        _, Co, co, _ = oracle.km_iterate(X, C0, repair=False)
+        assert list(counts[3:]) == [0, 0] and np.array_equal(counts, co)
+        np.testing.assert_array_equal(C[3:], X[:2].astype(np.float64))
+        np.testing.assert_allclose(C[:3], Co[:3], rtol=1e-13, atol=1e-13)
+        C[4] = 1e6
+        _, counts = km.ComputeMSEAndCorrectCounts(C)
+        assert counts[4] == 0
+        np.testing.assert_array_equal(C[4], X[2].astype(np.float64))
+
+
 @pytest.mark.parametrize("n", [1, 255, 257, 10001])
 def test_km_ragged(gpu_lib, oracle, n):
     X, _ = synth.kmeans_blobs(seed=8, n=max(n, 16), d=16, k=5)
