@@ -199,6 +199,7 @@ int main(int argc, char *argv[]) {
       A.SetParameters(maxiter, eps, athr, reg);
       t0 = clk::now();
       LogL = A.TrainNoCopy(G, verbosity, svd);
+      if (verbosity > 3) G.Dump();   // EM2/main.cpp: the fitted mixture
     } catch (EMException &e) {
       std::printf("EM algorithm failed: %s\n", e.what());
     }

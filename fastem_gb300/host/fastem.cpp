@@ -360,6 +360,11 @@ void CudaEM::RetrieveClasses(std::vector<int32_t> &classes) const {
   check(fem_em_retrieve_classes(h, classes.data()));
 }
 
+void CudaEM::ComputePosterriorCorrelation(std::vector<double> &corr) const {
+  corr.resize((size_t)K * K);
+  check(fem_em_posterior_correlation(h, corr.data()));
+}
+
 const char *CudaEM::GetName() const { return "cudaem (GB300 tcgen05)"; }
 
 // ---------------------------------------------------------------- k-means

@@ -120,8 +120,13 @@ class CudaEM {
   double Train(const Dataset &data, GaussianMixture &G, int verbosity, bool svd);
   double TrainNoCopy(GaussianMixture &G, int verbosity, bool svd);
   int GetIterCounter() const { return iterCounter; }
+  void ClearIterCounter() { iterCounter = 0; }
+  int GetK() const { return K; }
   const std::vector<double> &LogLikeTrace() const { return logl; }
   void RetrieveClasses(std::vector<int32_t> &classes) const;
+  // EMAlgorithm::ComputePosterriorCorrelation (EM2/EMAlgorithm.cpp:213-219):
+  // R^T R (K x K, row-major) over the posteriors of the last E-step
+  void ComputePosterriorCorrelation(std::vector<double> &corr) const;
   const char *GetName() const;
   fem_em *Handle() const { return h; }
 

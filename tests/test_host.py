@@ -102,6 +102,11 @@ def test_em2gpu_fp64_matches_oracle(em2gpu, oracle, tmp_path):
     np.testing.assert_allclose(G.covs, ref["sigma"], rtol=1e-9, atol=1e-12)
     cls = formats.read_classes(fc)
     assert cls.shape == (len(X),) and cls.min() >= 1 and cls.max() <= 3
+    # verbosity > 3 prints the fitted mixture (GaussianMixture::Dump) as em2 does
+    loud = subprocess.run([em2gpu, fb, "-c", "3", "-I", fi, "-p", "fp64", "-m", "2", "-v", "4"],
+                          capture_output=True, text=True, timeout=300)
+    assert loud.returncode == 0 and loud.stdout.count("Covariance matrix\n") == 3
+    assert "Condition number of the solution:" in loud.stdout
 
 
 @pytest.mark.gpu
