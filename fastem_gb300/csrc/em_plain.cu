@@ -149,6 +149,142 @@ k_estep_plain_generic(const float *__restrict__ X, int64_t n, int d, int K,
   if (tid == 0) part[blockIdx.x] = s;
 }
 
+// register-tiled form for d > 64: a CTA of 256 threads takes P = 32 PT
+// points.  Per component the centred points are staged once, transposed
+// (sT[m][p], pitch P + 1), and L^-1 is streamed through 64 x 64 chunks
+// (sW[m][o], pitch 68) up to the diagonal: output chunk o0 needs columns
+// m < o0 + 64 only (the factor's upper triangle is stored as zeros, so the
+// diagonal chunk needs no mask).  Thread (tp, to) = (tid / 8, tid % 8)
+// holds y for points tp + 32 i (i < PT) and outputs o0 + 8 to + (0..7): per
+// column m, PT broadcast loads of t and one 8-wide load of W feed 8 PT FMAs.
+// s = ||y||^2 is summed per thread over its outputs, then over the 8 threads
+// of a point group by a fixed shuffle tree (run-to-run reproducible).
+constexpr int kETileOC = 64;              // outputs per chunk
+constexpr int kETileMC = 64;              // factor columns per chunk
+constexpr int kETileWP = kETileOC + 4;    // sW pitch (16-byte rows)
+constexpr size_t kMaxDynSmem = 232448;    // opt-in shared memory per CTA (227 KB)
+
+// 8 consecutive elements from a 16-byte-aligned shared-memory address
+__device__ __forceinline__ void load8(const float *p, float (&v)[8]) {
+  const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+  v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+}
+__device__ __forceinline__ void load8(const double *p, double (&v)[8]) {
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[q];
+    v[2 * q] = a.x, v[2 * q + 1] = a.y;
+  }
+}
+
+template <typename T, int PT>
+constexpr size_t estep_tiled_smem(int d) {
+  return ((size_t)((d + 63) & ~63) * (32 * PT + 1) + (size_t)kETileMC * kETileWP + 32 * PT) * sizeof(T);
+}
+
+template <typename T, int PT>
+__global__ void __launch_bounds__(256)
+k_estep_plain_tiled(const float *__restrict__ X, int64_t n, int d, int K, const T *__restrict__ mu,
+                    const T *__restrict__ W, const T *__restrict__ logc, T *__restrict__ R,
+                    double *__restrict__ part) {
+  constexpr int P = 32 * PT, TP = P + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int dpad = (d + 63) & ~63;
+  T *sW = (T *)smem_raw;                       // kETileMC x kETileWP (first: 16-byte aligned rows)
+  T *sT = sW + kETileMC * kETileWP;            // dpad x TP
+  T *sLse = sT + (size_t)dpad * TP;            // P
+  __shared__ double red[8];
+  const int tid = threadIdx.x, to = tid & 7, tp = tid >> 3;
+  const int64_t i0 = (int64_t)blockIdx.x * P;
+  T mx[PT], se[PT];
+#pragma unroll
+  for (int i = 0; i < PT; i++) mx[i] = -INFINITY, se[i] = T(0);
+  for (int j = 0; j < K; j++) {
+    const T *mj = mu + (size_t)j * d;
+    const T *Wj = W + (size_t)j * d * d;
+    __syncthreads();                           // the previous component's reads of sT are done
+    // coalesced rows of X (column fastest); pitch TP puts consecutive
+    // columns of one point in consecutive banks
+    for (int e = tid; e < P * dpad; e += 256) {
+      const int p = e / dpad, m = e - p * dpad;
+      T t = T(0);
+      if (m < d && i0 + p < n) t = (T)X[(i0 + p) * d + m] - mj[m];
+      sT[(size_t)m * TP + p] = t;
+    }
+    T s[PT];
+#pragma unroll
+    for (int i = 0; i < PT; i++) s[i] = T(0);
+    for (int o0 = 0; o0 < dpad; o0 += kETileOC) {
+      T y[PT][8];
+#pragma unroll
+      for (int i = 0; i < PT; i++)
+#pragma unroll
+        for (int o = 0; o < 8; o++) y[i][o] = T(0);
+      for (int m0 = 0; m0 <= o0; m0 += kETileMC) {
+        __syncthreads();                       // sW free (and sT staged, on the first chunk)
+        for (int e = tid; e < kETileOC * kETileMC; e += 256) {
+          const int o = e / kETileMC, m = e - o * kETileMC;
+          const int go = o0 + o, gm = m0 + m;
+          sW[m * kETileWP + o] = (go < d && gm < d) ? Wj[(size_t)go * d + gm] : T(0);
+        }
+        __syncthreads();
+        const T *tcol = sT + (size_t)m0 * TP + tp;
+        const T *wrow = sW + to * 8;
+#pragma unroll 4
+        for (int m = 0; m < kETileMC; m++) {
+          T tv[PT], wv[8];
+#pragma unroll
+          for (int i = 0; i < PT; i++) tv[i] = tcol[(size_t)m * TP + 32 * i];
+          load8(wrow + m * kETileWP, wv);
+#pragma unroll
+          for (int i = 0; i < PT; i++)
+#pragma unroll
+            for (int o = 0; o < 8; o++) y[i][o] = fma(tv[i], wv[o], y[i][o]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < PT; i++)
+#pragma unroll
+        for (int o = 0; o < 8; o++) s[i] = fma(y[i][o], y[i][o], s[i]);
+    }
+    // the 8 threads of a point group are 8 consecutive lanes
+#pragma unroll
+    for (int i = 0; i < PT; i++) {
+      s[i] += __shfl_xor_sync(0xffffffffu, s[i], 1);
+      s[i] += __shfl_xor_sync(0xffffffffu, s[i], 2);
+      s[i] += __shfl_xor_sync(0xffffffffu, s[i], 4);
+    }
+    if (to == 0) {
+      const T lc = logc[j];
+#pragma unroll
+      for (int i = 0; i < PT; i++) {
+        const int64_t pi = i0 + tp + 32 * i;
+        const T l = lc - T(0.5) * s[i];
+        if (pi < n) R[(size_t)j * n + pi] = l;
+        lse_push(l, mx[i], se[i]);
+      }
+    }
+  }
+  double v = 0.0;
+  if (to == 0)
+#pragma unroll
+    for (int i = 0; i < PT; i++) {
+      const T lse = mx[i] + t_log(se[i]);
+      sLse[tp + 32 * i] = lse;
+      if (i0 + tp + 32 * i < n) v += (double)lse;
+    }
+  __syncthreads();                             // sLse and every l_ij of this CTA written
+  for (int e = tid; e < K * P; e += 256) {
+    const int j = e / P, p = e - j * P;
+    if (i0 + p < n) {
+      T *q = R + (size_t)j * n + i0 + p;
+      *q = t_exp(*q - sLse[p]);
+    }
+  }
+  const double ls = block_sum<256>(v, red);
+  if (tid == 0) part[blockIdx.x] = ls;
+}
+
 // single-block deterministic sum of the per-block log-likelihood partials
 __global__ void __launch_bounds__(1024) k_reduce_logl(const double *part, int64_t np, DevStatus *st) {
   __shared__ double red[32];
@@ -457,11 +593,19 @@ static int estep_plain_t(fem_em *h) {
     FEM_EPL(32)
     FEM_EPL(64)
     default: {
-      nb = (n + 63) / 64;
-      size_t sm = (size_t)64 * (d + 1) * sizeof(T);
-      FEM_CUDA(allow_dyn_smem(k_estep_plain_generic<T>, sm));
-      k_estep_plain_generic<T><<<(unsigned)nb, 64, sm, s>>>(h->X, n, d, K, mu, W, lc, R,
-                                                            h->logl_part);
+      constexpr int PT = sizeof(T) == 4 ? 4 : 2;   // 128 FP32 or 64 FP64 points per CTA
+      const size_t smt = estep_tiled_smem<T, PT>(d);
+      if (d > 64 && smt <= kMaxDynSmem) {
+        nb = (n + 32 * PT - 1) / (32 * PT);
+        FEM_CUDA(allow_dyn_smem(k_estep_plain_tiled<T, PT>, smt));
+        k_estep_plain_tiled<T, PT><<<(unsigned)nb, 256, smt, s>>>(h->X, n, d, K, mu, W, lc, R, h->logl_part);
+      } else {
+        nb = (n + 63) / 64;
+        size_t sm = (size_t)64 * (d + 1) * sizeof(T);
+        FEM_CUDA(allow_dyn_smem(k_estep_plain_generic<T>, sm));
+        k_estep_plain_generic<T><<<(unsigned)nb, 64, sm, s>>>(h->X, n, d, K, mu, W, lc, R,
+                                                              h->logl_part);
+      }
     }
   }
 #undef FEM_EPL

@@ -235,10 +235,14 @@ def test_concurrent_handles_of_different_shapes(gpu_lib, precision):
         np.testing.assert_array_equal(tr, alone[j % len(shapes)])
 
 
-@pytest.mark.parametrize("d,precision", [(2, "fp64"), (5, "fp32"), (13, "fp64"), (37, "fp32"), (63, "fp64")])
+@pytest.mark.parametrize("d,precision", [(2, "fp64"), (5, "fp32"), (13, "fp64"), (37, "fp32"), (63, "fp64"),
+                                         (80, "fp64"), (100, "fp32"), (130, "fp64"), (256, "fp32"),
+                                         (256, "fp64")])
 def test_plain_forms_any_dimension(gpu_lib, oracle, d, precision):
     """The CUDA-core forms at dimensions that are not powers of two: ragged
-    column chunks in the means sums, 1- and 2-wide covariance tiles."""
+    column chunks in the means sums, 1- and 2-wide covariance tiles; above
+    d = 64 the register-tiled E-step (ragged last 64-wide chunk at d = 80,
+    100 and 130)."""
     X, _ = synth.kmeans_blobs(seed=900 + d, n=6000, d=d, k=5, spread=8.0)
     init = synth.dsquared_init(X, 5, seed=d)
     ref = oracle.em_train(X, *init, 4, eps=0.0, abort_thr=1e12)
@@ -251,5 +255,8 @@ def test_plain_forms_any_dimension(gpu_lib, oracle, d, precision):
         np.testing.assert_allclose(got["mu"], ref["mu"], rtol=1e-9, atol=1e-10 * scale)
         np.testing.assert_allclose(got["sigma"], ref["sigma"], rtol=1e-8, atol=1e-10)
     else:
-        assert err <= 1e-5
+        # FP32 log densities are of magnitude ~d and rounded at 2^-24 of it:
+        # an FP32 E-step emulated in numpy on the d = 256 case differs from
+        # FP64 by |dlogL/N| = 3.9e-5, so the bar grows with d above d = 50
+        assert err <= max(1e-5, 2e-7 * d)
         assert np.max(np.abs(got["mu"] - ref["mu"])) <= 1e-4 * scale
