@@ -433,16 +433,19 @@ struct PostHiLo {
 template <typename T, int TB, class Src>
 __global__ void __launch_bounds__(256)
 k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T *__restrict__ mu, int mu_ld,
-            double *__restrict__ part, int nb, int nblk, int64_t rows_per_chunk) {
+            double *__restrict__ part, int nb, int nblk, int64_t rows_per_chunk, int upc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *sZ = (T *)smem_raw;  // CJ x TP x d
   const int tid = threadIdx.x;
-  const int u0 = blockIdx.x * 256;
+  // this CTA's upc (<= 256, a multiple of 32) units; the components they
+  // span are staged, so small d with many components takes fewer units
+  const int u0 = blockIdx.x * upc;
   const int j_lo = u0 / nblk;
-  const int j_hi = min(K - 1, (u0 + 255) / nblk);
+  const int j_hi = min(K - 1, (u0 + upc - 1) / nblk);
   const int CJ = j_hi - j_lo + 1;
+  T *sSr = sZ + (size_t)CJ * kCovTP * d;  // CJ x TP: sqrt(r), once per point and component
   const int unit = u0 + tid;
-  const bool valid = unit < K * nblk;
+  const bool valid = tid < upc && unit < K * nblk;
   int j = 0, bi = 0, bj = 0;
   if (valid) {
     j = unit / nblk;
@@ -473,6 +476,11 @@ k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T
   for (int64_t t0 = c0; t0 < c1; t0 += kCovTP) {
     const int tp = (int)min((int64_t)kCovTP, c1 - t0);
     __syncthreads();
+    for (int e = tid; e < CJ * kCovTP; e += 256) {
+      const int jj = e / kCovTP, p = e - jj * kCovTP;
+      sSr[e] = p < tp ? sqrt((T)R(j_lo + jj, t0 + p)) : T(0);
+    }
+    __syncthreads();
     const int tot = CJ * kCovTP * d;
     for (int e = tid; e < tot; e += 256) {
       const int jj = e / (kCovTP * d);
@@ -481,8 +489,7 @@ k_cov_plain(const float *__restrict__ X, int64_t n, int d, int K, Src R, const T
       T z = T(0);
       if (p < tp) {
         const int64_t row = t0 + p;
-        const T r = (T)R(j_lo + jj, row);
-        z = sqrt(r) * ((T)X[row * d + a] - mu[(size_t)(j_lo + jj) * mu_ld + a]);
+        z = sSr[jj * kCovTP + p] * ((T)X[row * d + a] - mu[(size_t)(j_lo + jj) * mu_ld + a]);
       }
       sZ[e] = z;
     }
@@ -656,13 +663,22 @@ static int launch_means(fem_em *h, int upt, int64_t rpb, size_t sm) {
 template <typename T, int TB, class Src>
 static int launch_cov(fem_em *h, int nb, int nblk, int64_t rpc, Src src, const T *mu, int mu_ld) {
   const int units = h->k * nblk;
-  const int gx = (units + 255) / 256;
-  const int cjmax = 256 / nblk + 2;
-  size_t sm = (size_t)min(cjmax, h->k) * kCovTP * h->d * sizeof(T);
+  // z tiles + sqrt(r) of the components that upc consecutive units span
+  auto smem = [&](int upc) {
+    return (size_t)min((upc - 1) / nblk + 2, h->k) * kCovTP * (h->d + 1) * sizeof(T);
+  };
+  int upc = 256;
+  while (upc > 32 && smem(upc) > kMaxDynSmem) upc -= 32;
+  if (smem(upc) > kMaxDynSmem) {
+    set_error("covariance tiles of d = %d need %zu bytes of shared memory", h->d, smem(upc));
+    return FEM_ERR_UNSUPPORTED;
+  }
+  const size_t sm = smem(upc);
+  const int gx = (units + upc - 1) / upc;
   FEM_CUDA(allow_dyn_smem(k_cov_plain<T, TB, Src>, sm));
   dim3 grid(gx, h->cchunks);
   k_cov_plain<T, TB, Src><<<grid, 256, sm, h->stream>>>(h->X, h->n, h->d, h->k, src, mu, mu_ld, h->cpart, nb,
-                                                        nblk, rpc);
+                                                        nblk, rpc, upc);
   return FEM_OK;
 }
 

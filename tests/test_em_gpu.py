@@ -235,6 +235,23 @@ def test_concurrent_handles_of_different_shapes(gpu_lib, precision):
         np.testing.assert_array_equal(tr, alone[j % len(shapes)])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_plain_many_components_small_d(gpu_lib, oracle, precision):
+    """K = 256 components of d = 4: a covariance CTA stages the z tiles of
+    every component its units span, so with many components per CTA it
+    takes fewer units (FP64 needed more than a CTA's shared memory here
+    before)."""
+    X, _ = synth.kmeans_blobs(seed=950, n=40000, d=4, k=256, spread=8.0)
+    init = synth.dsquared_init(X, 256, seed=50)
+    ref = oracle.em_train(X, *init, 3, eps=0.0, abort_thr=1e12)
+    assert ref["status"] == 0
+    got = run_gpu(X, init, 3, precision)
+    err = np.max(np.abs(got["logl"] - ref["logl"])) / len(X)
+    assert err <= (1e-11 if precision == "fp64" else 1e-5), err
+    if precision == "fp64":
+        np.testing.assert_allclose(got["sigma"], ref["sigma"], rtol=1e-8, atol=1e-10)
+
+
 @pytest.mark.parametrize("d,precision", [(2, "fp64"), (5, "fp32"), (13, "fp64"), (37, "fp32"), (63, "fp64"),
                                          (80, "fp64"), (100, "fp32"), (130, "fp64"), (256, "fp32"),
                                          (256, "fp64")])
