@@ -43,6 +43,60 @@ class GaussianMixture:
     def copy(self):
         return GaussianMixture(self.weights, self.means, self.covs)
 
+    def _log_terms(self, X):
+        """log(pi_j N(x; mu_j, Sigma_j)) for the rows of X (n x K, FP64 on the
+        host), through the Cholesky factor of each covariance's lower triangle
+        as NormalDensity::Init (EM2/NormalDensity.cpp:43-65) forms it."""
+        X = np.atleast_2d(np.asarray(X, dtype=np.float64))
+        k, d = self.means.shape
+        out = np.empty((X.shape[0], k))
+        for j in range(k):
+            L = np.linalg.cholesky(np.tril(self.covs[j]) + np.tril(self.covs[j], -1).T)
+            y = np.linalg.solve(L, (X - self.means[j]).T)
+            logdet = 2.0 * np.log(np.diag(L)).sum()
+            out[:, j] = (np.log(self.weights[j]) - 0.5 * d * np.log(2.0 * np.pi) - 0.5 * logdet
+                         - 0.5 * np.einsum("ij,ij->j", y, y))
+        return out
+
+    def Evaluate(self, x):
+        """GaussianMixture::Evaluate (EM2/GaussianMixture.cpp:54-60): the
+        mixture density sum_j pi_j N(x), summed in the log domain (the same
+        value where the densities do not underflow).  One row -> a float,
+        n rows -> n values."""
+        lt = self._log_terms(x)
+        m = lt.max(axis=1, keepdims=True)
+        v = (np.exp(m[:, 0]) * np.exp(lt - m).sum(axis=1))
+        return float(v[0]) if np.ndim(x) == 1 else v
+
+    def ComputePosteriors(self, x):
+        """GaussianMixture::ComputePosteriors (EM2/GaussianMixture.cpp:62-69):
+        pi_j N(x) / sum, per row."""
+        lt = self._log_terms(x)
+        p = np.exp(lt - lt.max(axis=1, keepdims=True))
+        p /= p.sum(axis=1, keepdims=True)
+        return p[0] if np.ndim(x) == 1 else p
+
+    def Classify(self, x):
+        """GaussianMixture::Classify (EM2/GaussianMixture.cpp:86-98): the
+        component of largest pi_j N(x), lowest index on ties; compared in the
+        log domain, so a row far from every component still gets its nearest
+        one where the reference's densities underflow to 0 and give 0."""
+        c = np.argmax(self._log_terms(x), axis=1)
+        return int(c[0]) if np.ndim(x) == 1 else c
+
+    def NormalizeWeights(self):
+        """GaussianMixture::NormalizeWeights (EM2/GaussianMixture.cpp:71-79)."""
+        self.weights *= 1.0 / self.weights.sum()
+
+    def FindLargestConditionNumber(self):
+        """GaussianMixture::FindLargestConditionNumber (EM2/GaussianMixture.cpp:
+        125-135): max(1, |lambda_max / lambda_min|) over the covariances."""
+        cond = 1.0
+        for S in self.covs:
+            ev = np.linalg.eigvalsh(S, UPLO="L")
+            cond = max(cond, abs(ev[-1] / ev[0]))
+        return cond
+
 
 class CudaMatrixEM:
     """EMAlgorithm with every sweep on the GPU.
