@@ -81,9 +81,12 @@ class GaussianMixture {
   const std::vector<double> &Means() const { return means; }
   const std::vector<double> &Covs() const { return covs; }
 
-  // log p(x) of the mixture and argmax_j of pi_j N(x; mu_j, Sigma_j)
-  // (GaussianMixture::Evaluate / Classify, EM2/GaussianMixture.cpp:54-109),
-  // FP64 on the host, one Cholesky per component on first use
+  // the mixture density sum_j pi_j N(x; mu_j, Sigma_j) and the argmax_j of
+  // its terms, lowest index on ties (GaussianMixture::Evaluate / Classify,
+  // EM2/GaussianMixture.cpp:54-98), FP64 on the host, one Cholesky per
+  // component on first use.  Both work in the log domain: where every
+  // density underflows to 0 (a row far from all components) the reference's
+  // Classify returns 0, this one the component of largest log(pi_j N(x))
   double Evaluate(const float *x) const;
   int Classify(const float *x) const;
 
