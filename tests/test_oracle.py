@@ -21,6 +21,33 @@ def test_rng_known_answer(oracle):
     assert oracle.rng_uniform() == float(9981545732273789042) / 2.0 ** 64
 
 
+REF_RAND = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "ref_rand")
+
+
+@pytest.mark.parametrize("seed", [0, 2, 3, 11, 637563561, 4294967295])
+def test_rng_matches_reference_rand(oracle, seed):
+    """The oracle's generator against the reference's own Util/Rand.cpp
+    (compiled in place into oracle/_ref where the reference sources are
+    present): SRand(seed), then Rand() and RandInt(n) bit for bit."""
+    import subprocess
+    if not os.access(REF_RAND, os.X_OK):
+        pytest.skip("oracle/_ref/ref_rand not built (reference sources absent)")
+    count, n = 2000, 1000003
+    try:
+        out = subprocess.run([REF_RAND, str(seed), str(count), str(n)], capture_output=True, text=True,
+                             timeout=60)
+    except OSError as e:                       # built for another CPU architecture
+        pytest.skip(str(e))
+    vals = out.stdout.split()
+    ref_u = [float(v) for v in vals[:count]]
+    ref_i = [int(v) for v in vals[count:]]
+    oracle.rng_seed(seed)
+    got_u = [oracle.rng_uniform() for _ in range(count)]
+    got_i = [int(oracle.rng_uniform() * n) for _ in range(count)]
+    assert got_u == ref_u
+    assert got_i == ref_i
+
+
 def test_rng_golden(oracle):
     z = np.load(os.path.join(GOLDEN, "rng.npz"))
     oracle.rng_seed(42)
