@@ -386,7 +386,6 @@ int upload_km(fem_km *h, const float *X, int64_t ld, cudaMemcpyKind kind) {
   }
   h->xg2 = 0.0;
   for (double v : hp) h->xg2 += v;
-  if (h->cfg.precision == FEM_PREC_MIXED) FEM_TRY(km_tc_upload(h));
   h->have_data = true;
   return FEM_OK;
 }

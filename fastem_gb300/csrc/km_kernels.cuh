@@ -13,7 +13,6 @@ size_t km_assign_smem(int K, int D);
 bool km_tc_supported(int d, int k);
 int km_tc_create(fem_km *h);
 void km_tc_destroy(fem_km *h);
-int km_tc_upload(fem_km *h);
 int km_tc_assign(fem_km *h);
 
 }  // namespace fem

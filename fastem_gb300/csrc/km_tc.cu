@@ -482,8 +482,6 @@ void km_tc_destroy(fem_km *h) {
   h->tc = nullptr;
 }
 
-int km_tc_upload(fem_km *h) { return FEM_OK; }
-
 int km_tc_assign(fem_km *h) {
   KmTcPlanImpl *p = static_cast<KmTcPlanImpl *>(h->tc);
   FEM_CUDA(cudaMemsetAsync(p->cconst + 3 * p->kp, 0, 2 * sizeof(float), h->stream));
