@@ -64,7 +64,15 @@ def read_cmp(fname):
 
 
 def read_classes(fname):
+    """A classes file (GaussianMixture::WriteClasses, EM2/GaussianMixture.cpp;
+    read as ReadAssignment, Util/MultithreadedDataset.cpp:371-386): an int32
+    count, or -1 and an int64 count, then the 1-based int32 classes, returned
+    as stored (1-based)."""
     with open(fname, "rb") as f:
         n = int(np.fromfile(f, dtype=np.int32, count=1)[0])
+        if n == -1:
+            n = int(np.fromfile(f, dtype=np.int64, count=1)[0])
         c = np.fromfile(f, dtype=np.int32, count=n)
+    if len(c) != n:
+        raise ValueError("%s: %d of %d classes" % (fname, len(c), n))
     return c

@@ -75,6 +75,27 @@ def test_cmp_read_by_cpp(em2gpu, tmp_path):
     assert float(d["sum_covs"]) == pytest.approx(G.covs.sum(), rel=1e-12)
 
 
+def test_classes_file_both_headers(tmp_path):
+    """Classes files as ReadAssignment reads them: an int32 count, or -1 and
+    an int64 count, then 1-based int32 classes; a short file is refused."""
+    cls = np.array([1, 3, 2, 2, 1], dtype=np.int32)
+    short, long_, bad = (str(tmp_path / n) for n in ("s.cls", "l.cls", "b.cls"))
+    with open(short, "wb") as f:
+        np.array([5], dtype=np.int32).tofile(f)
+        cls.tofile(f)
+    with open(long_, "wb") as f:
+        np.array([-1], dtype=np.int32).tofile(f)
+        np.array([5], dtype=np.int64).tofile(f)
+        cls.tofile(f)
+    with open(bad, "wb") as f:
+        np.array([7], dtype=np.int32).tofile(f)
+        cls.tofile(f)
+    np.testing.assert_array_equal(formats.read_classes(short), cls)
+    np.testing.assert_array_equal(formats.read_classes(long_), cls)
+    with pytest.raises(ValueError):
+        formats.read_classes(bad)
+
+
 def test_usage_without_arguments(em2gpu):
     out = subprocess.run([em2gpu], capture_output=True, text=True, timeout=60)
     assert out.returncode == 1 and "Arguments" in out.stdout
