@@ -11,6 +11,7 @@
 // -o writes the fitted mixture (.cmp), -O the classes of every row under the
 // fitted mixture, 1-based, after an int32 row count (GaussianMixture::WriteClasses).
 #include <chrono>
+#include <climits>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -213,10 +214,14 @@ int main(int argc, char *argv[]) {
     if (cname) {
       FILE *f = std::fopen(cname, "wb");
       if (!f) throw FileException(std::string("cannot create ") + cname);
-      const int32_t n = (int32_t)D.GetRowCount();
-      std::vector<int32_t> cls(D.GetRowCount());
-      for (int64_t i = 0; i < D.GetRowCount(); i++) cls[i] = G.Classify(D.GetRow(i)) + 1;
-      const bool ok = std::fwrite(&n, 4, 1, f) == 1 && std::fwrite(cls.data(), 4, cls.size(), f) == cls.size();
+      // an int32 count, or -1 and an int64 count above 2^31 - 1 rows (the
+      // two forms ReadAssignment reads, Util/MultithreadedDataset.cpp:371-386)
+      const int64_t rows = D.GetRowCount();
+      const int32_t n32 = rows > INT32_MAX ? -1 : (int32_t)rows;
+      std::vector<int32_t> cls(rows);
+      for (int64_t i = 0; i < rows; i++) cls[i] = G.Classify(D.GetRow(i)) + 1;
+      bool ok = std::fwrite(&n32, 4, 1, f) == 1 && (n32 != -1 || std::fwrite(&rows, 8, 1, f) == 1);
+      ok = ok && std::fwrite(cls.data(), 4, cls.size(), f) == cls.size();
       std::fclose(f);
       if (!ok) throw FileException("write failed");
     }
