@@ -60,6 +60,22 @@ def test_bad_arguments_rejected(gpu_lib):
     assert "null" in C.last_error()
 
 
+def test_km_repair_modes_and_rng_state_arguments(gpu_lib):
+    """The k-means repair modes are checked before any device work, and the
+    repair-generator state calls refuse a missing handle."""
+    from fastem_gb300 import _capi as C
+    kc = C.KmConfig()
+    gpu_lib.fem_km_config_default(ctypes.byref(kc))
+    assert kc.repair == 1                                   # FEM_KM_REPAIR_RANDOM
+    kc.precision, kc.repair = C.PREC["fp32"], 3
+    h = ctypes.c_void_p()
+    assert gpu_lib.fem_km_create(8, 1000, 4, ctypes.byref(kc), ctypes.byref(h)) == C.FEM_ERR_BAD_ARG
+    assert "repair" in C.last_error() and not h.value
+    assert gpu_lib.fem_km_set_rng_state(None, b"1 2 3") == C.FEM_ERR_BAD_ARG
+    buf = ctypes.create_string_buffer(16)
+    assert gpu_lib.fem_km_get_rng_state(None, buf, 16) == C.FEM_ERR_BAD_ARG
+
+
 def test_python_binding_raises_when_library_missing(monkeypatch, tmp_path):
     from fastem_gb300 import _capi
     monkeypatch.setattr(_capi, "_LIB", None)
