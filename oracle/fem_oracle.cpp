@@ -4,9 +4,12 @@
  * configurations start from.
  *
  * TEST INFRASTRUCTURE ONLY (see fem_oracle.h): the checker and the timed CPU
- * baseline, never part of the shipped library.  PARITY UNPINNED: the
- * reference cannot be built here and has no golden vectors; this code is
- * cross-checked against an independent numpy/scipy FP64 computation.
+ * baseline, never part of the shipped library.  PARITY UNPINNED for the EM
+ * and k-means arithmetic: the reference cannot be built here and has no
+ * golden vectors; this code is cross-checked against an independent
+ * numpy/scipy FP64 computation.  The generator stream (orc_rng_*) is pinned:
+ * it equals the reference's own Util/Rand.cpp, compiled in place by
+ * `make ref` (Makefile), bit for bit.
  *
  * Arithmetic notes.  Everything is IEEE double with sequential summation in
  * index order; the file is compiled with -ffp-contract=off so x86 and Arm

@@ -3,10 +3,12 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline legs, never by the fastem_gb300 package.
 
-PARITY UNPINNED: the reference (wkwedlo/fastem) cannot be built here (Eigen,
-MKL, libnuma and MPI are absent) and ships no golden vectors; the oracle is
-cross-checked against an independent numpy FP64 computation instead
-(tests/test_oracle.py).
+PARITY UNPINNED for the EM and k-means arithmetic: the reference
+(wkwedlo/fastem) cannot be built here (Eigen, MKL, libnuma and MPI are
+absent) and ships no golden vectors; the oracle is cross-checked against an
+independent numpy FP64 computation instead (tests/test_oracle.py).  The
+generator stream is pinned against the reference's own Util/Rand.cpp,
+compiled in place (`make -C oracle ref`) where its sources are present.
 """
 import ctypes
 import os
