@@ -274,6 +274,7 @@ def test_plain_forms_any_dimension(gpu_lib, oracle, d, precision):
     else:
         # FP32 log densities are of magnitude ~d and rounded at 2^-24 of it:
         # an FP32 E-step emulated in numpy on the d = 256 case differs from
-        # FP64 by |dlogL/N| = 3.9e-5, so the bar grows with d above d = 50
+        # FP64 by |dlogL/N| = 3.9e-5 (test_fp32_model.py), so the bar grows
+        # with d above d = 50
         assert err <= max(1e-5, 2e-7 * d)
         assert np.max(np.abs(got["mu"] - ref["mu"])) <= 1e-4 * scale
