@@ -181,6 +181,13 @@ int main(int argc, char *argv[]) {
     std::printf("EM abort threshold: %g\n", athr);
     Rand rnd(seed);
     GaussianMixture G = InitMixture(iname, D, ncl, rnd, precision, device);
+    if (G.GetComponentCount() != ncl || G.GetDimension() != D.GetColCount()) {
+      // a .cmp initial mixture must match -c and the dataset (the reference
+      // would read past the mixture in DecodeMixture)
+      std::fprintf(stderr, "em2gpu: the initial mixture has %d components of dimension %d; -c %d on %d columns\n",
+                   G.GetComponentCount(), G.GetDimension(), ncl, D.GetColCount());
+      return 1;
+    }
     CudaEM A(D.GetColCount(), D.GetRowCount(), ncl, precision, device);
     std::printf("Using EM algorithm %s\n", A.GetName());
     double LogL = 0.0;

@@ -96,6 +96,22 @@ def test_classes_file_both_headers(tmp_path):
         formats.read_classes(bad)
 
 
+def test_em2gpu_refuses_mismatched_initial_mixture(em2gpu, tmp_path):
+    """-I file.cmp with another component count than -c, or another
+    dimension than the dataset's, stops before any GPU work."""
+    z = np.load(os.path.join(GOLDEN, "em_small.npz"))
+    fb, fi = str(tmp_path / "x.bin"), str(tmp_path / "g.cmp")
+    formats.write_bin(fb, z["X"])
+    formats.write_cmp(fi, GaussianMixture(z["pi0"], z["mu0"], z["sigma0"]))   # 3 components, d = 4
+    for c in ("2", "5"):
+        out = subprocess.run([em2gpu, fb, "-c", c, "-I", fi, "-m", "2"], capture_output=True, text=True, timeout=60)
+        assert out.returncode == 1 and "initial mixture has 3 components of dimension 4" in out.stderr
+    fw = str(tmp_path / "w.bin")
+    formats.write_bin(fw, np.zeros((50, 6), dtype=np.float32))
+    out = subprocess.run([em2gpu, fw, "-c", "3", "-I", fi, "-m", "2"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "on 6 columns" in out.stderr
+
+
 def test_usage_without_arguments(em2gpu):
     out = subprocess.run([em2gpu], capture_output=True, text=True, timeout=60)
     assert out.returncode == 1 and "Arguments" in out.stdout
