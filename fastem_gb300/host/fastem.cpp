@@ -7,6 +7,7 @@
 #include <cstring>
 #include <sstream>
 #include <thread>
+#include <unordered_set>
 
 namespace fastem {
 
@@ -597,16 +598,18 @@ GaussianMixture InitMixture(const char *name, const Dataset &data, int K, Rand &
     // draw misses the rows already taken, but keeps the first draw (the
     // repeat test reads a shadowing variable): the same rows and the same
     // use of the stream here, repeats included.
+    // Once the rows taken cover all N rows no draw can miss them: the
+    // reference loops forever there (K > N); here the redraws stop.
     GaussianMixture G(K, d);
     const double cv = data.GetCovMatrixTrace() / d / 10.0;
-    std::vector<int64_t> taken;
+    std::unordered_set<int64_t> taken;
     for (int j = 0; j < K; j++) {
       const int64_t idx = (int64_t)(rnd() * (double)N);
-      for (;;) {
+      while ((int64_t)taken.size() < N) {
         const int64_t again = (int64_t)(rnd() * (double)N);
-        if (std::find(taken.begin(), taken.end(), again) == taken.end()) break;
+        if (!taken.count(again)) break;
       }
-      taken.push_back(idx);
+      taken.insert(idx);
       for (int q = 0; q < d; q++) G.Means()[(size_t)j * d + q] = data.GetRow(idx)[q];
       for (int a = 0; a < d; a++)
         for (int b = 0; b < d; b++) G.Covs()[((size_t)j * d + a) * d + b] = a == b ? cv : 0.0;

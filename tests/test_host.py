@@ -223,7 +223,9 @@ def jain_rows(n, k, seed, oracle):
     taken = []
     for _ in range(k):
         idx = int(oracle.rng_uniform() * n)
-        while int(oracle.rng_uniform() * n) in taken:
+        # once every row is taken no draw can miss: the reference loops
+        # forever there, the host library stops redrawing
+        while len(set(taken)) < n and int(oracle.rng_uniform() * n) in taken:
             pass
         taken.append(idx)
     return taken
@@ -245,6 +247,19 @@ def test_eminit_jain(eminit, oracle, tmp_path):
     cv = np.trace(np.cov(X.astype(np.float64).T)) / 3 / 10
     np.testing.assert_allclose(G.covs, np.broadcast_to(np.eye(3) * cv, (7, 3, 3)), rtol=1e-12)
     np.testing.assert_array_equal(G.weights, np.full(7, 1.0 / 7))
+
+
+def test_eminit_jain_more_components_than_rows(eminit, oracle, tmp_path):
+    """K > N: the reference's repeat loop never ends once every row is
+    taken; here the draws stop there and the run completes."""
+    X = np.arange(15, dtype=np.float32).reshape(5, 3)
+    fb, fo = str(tmp_path / "s.bin"), str(tmp_path / "s.cmp")
+    formats.write_bin(fb, X)
+    out = subprocess.run([eminit, "-I", "jain", "-c", "8", "-r", "4", "-o", fo, fb], capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
+    G, _ = formats.read_cmp(fo)
+    np.testing.assert_array_equal(G.means, X[jain_rows(5, 8, 4, oracle)].astype(np.float64))
 
 
 def test_eminit_file_dump_and_arguments(eminit, tmp_path):
