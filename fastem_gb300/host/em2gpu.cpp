@@ -67,6 +67,13 @@ int info(const char *fname) {
   return 0;
 }
 
+// a refused option value: em2's message (EM2/main.cpp prints it after
+// "Invalid program argument: "), exit status 1
+int bad_argument(const char *msg) {
+  std::printf("Invalid program argument: %s\n", msg);
+  return 1;
+}
+
 }  // namespace
 
 // the seeders on the host (no GPU): K rows of %.17g coordinates
@@ -135,16 +142,37 @@ int main(int argc, char *argv[]) {
       case 'B':
         std::printf("-B benchmarks the reference's OpenMP reduction; the GPU backend has none\n");
         return 0;
-      case 'c': ncl = std::atoi(optarg); break;
+      // value checks and messages of ProcessArgs (EM2/EMArgs.cpp:75-170)
+      case 'c':
+        if ((ncl = std::atoi(optarg)) <= 0) return bad_argument("invalid value of -c option");
+        break;
       case 'I': iname = optarg; break;
-      case 'r': seed = (unsigned)std::atoi(optarg); break;
-      case 'm': maxiter = std::atoi(optarg); break;
-      case 'b': burnin = std::atoi(optarg); break;
-      case 'f': eps = std::atof(optarg); break;
-      case 'a': athr = std::atof(optarg); break;
-      case 'g': reg = std::atof(optarg); break;
+      case 'r': {
+        const int r = std::atoi(optarg);
+        if (r < 0) return bad_argument("invalid value of -r option");
+        seed = (unsigned)r;
+        break;
+      }
+      case 'm':
+        if ((maxiter = std::atoi(optarg)) < 0) return bad_argument("invalid value of -m option");
+        break;
+      case 'b':
+        if ((burnin = std::atoi(optarg)) < 0) return bad_argument("invalid value of -b option");
+        break;
+      case 'f':
+        if ((eps = std::atof(optarg)) <= 0.0) return bad_argument("argument to -f must be greater or than 0");
+        break;
+      case 'a':
+        if ((athr = std::atof(optarg)) < 1.0) return bad_argument("argument to -a must be greater then 1.0");
+        break;
+      case 'g':
+        reg = std::atof(optarg);
+        if (reg < 0.0 || reg > 1.0) return bad_argument("argument to -g must be small positive number");
+        break;
       case 'S': svd = false; break;
-      case 'v': verbosity = std::atoi(optarg); break;
+      case 'v':
+        if ((verbosity = std::atoi(optarg)) < 0) return bad_argument("invalid value of -v option");
+        break;
       case 'o': oname = optarg; break;
       case 'O': cname = optarg; break;
       case 'd': device = std::atoi(optarg); break;

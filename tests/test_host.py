@@ -96,6 +96,21 @@ def test_classes_file_both_headers(tmp_path):
         formats.read_classes(bad)
 
 
+@pytest.mark.parametrize("opt,val,msg", [("-c", "0", "invalid value of -c option"),
+                                          ("-r", "-1", "invalid value of -r option"),
+                                          ("-m", "-2", "invalid value of -m option"),
+                                          ("-b", "-1", "invalid value of -b option"),
+                                          ("-v", "-1", "invalid value of -v option"),
+                                          ("-f", "0", "argument to -f must be greater or than 0"),
+                                          ("-a", "0.5", "argument to -a must be greater then 1.0"),
+                                          ("-g", "1.5", "argument to -g must be small positive number")])
+def test_em2gpu_option_values_checked_as_em2(em2gpu, opt, val, msg):
+    """ProcessArgs' value checks (EM2/EMArgs.cpp:75-170), refused before the
+    dataset is read."""
+    out = subprocess.run([em2gpu, opt, val, "missing.bin"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "Invalid program argument: " + msg in out.stdout
+
+
 def test_em2gpu_refuses_mismatched_initial_mixture(em2gpu, tmp_path):
     """-I file.cmp with another component count than -c, or another
     dimension than the dataset's, stops before any GPU work."""
@@ -126,7 +141,8 @@ def test_em2gpu_fp64_matches_oracle(em2gpu, oracle, tmp_path):
     fb, fi, fo, fc = (str(tmp_path / n) for n in ("x.bin", "init.cmp", "out.cmp", "cls.bin"))
     formats.write_bin(fb, X)
     formats.write_cmp(fi, GaussianMixture(z["pi0"], z["mu0"], z["sigma0"]))
-    out = subprocess.run([em2gpu, fb, "-c", "3", "-I", fi, "-p", "fp64", "-m", "8", "-f", "0", "-v", "2",
+    # -f must be > 0 (as em2 requires): 1e-300 keeps all 8 sweeps, as eps = 0 in the oracle
+    out = subprocess.run([em2gpu, fb, "-c", "3", "-I", fi, "-p", "fp64", "-m", "8", "-f", "1e-300", "-v", "2",
                           "-o", fo, "-O", fc], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     ll = [float(l.split("LogL:")[1].split()[0]) for l in out.stdout.splitlines() if l.startswith("iter:")]
