@@ -36,8 +36,10 @@ def build():
         if head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") != want:
             os.remove(so)
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
-    # the reference's own generator, where its sources are present
-    subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
+    # the reference's own generator, where its sources are present (optional:
+    # the test that uses it skips without it)
+    subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=False, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
 
 
 def lib():
