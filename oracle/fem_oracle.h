@@ -113,6 +113,9 @@ void orc_km_forgy(int d, int64_t n, int k, const float *X, double *centroids);
  * pi, mu, sigma are updated in place; *logl is the pre-M-step logL. */
 int orc_em_sweep_blas(int d, int64_t n, int k, const float *X, double *pi, double *mu, double *sigma,
                       double *logl, int nthreads, void *dtrmm, void *dgemm, void *dsyrk);
+int orc_em_sweeps_blas(int d, int64_t n, int k, const float *X, double *pi, double *mu, double *sigma,
+                       int sweeps, int svd, double abort_thr, double *logl, double *seconds, int nthreads,
+                       void *dtrmm, void *dgemm, void *dsyrk);
 
 #ifdef __cplusplus
 }

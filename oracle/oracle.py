@@ -36,10 +36,12 @@ def build():
         if head[:4] == b"\x7fELF" and int.from_bytes(head[18:20], "little") != want:
             os.remove(so)
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
-    # the reference's own generator, where its sources are present (optional:
-    # the test that uses it skips without it)
-    subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=False, stdout=subprocess.DEVNULL,
-                   stderr=subprocess.DEVNULL)
+    # the reference's own generator and k-means, where its sources are present
+    # (optional: the tests that use them skip without them)
+    ref = os.environ.get("FEM_REFERENCE_DIR") or ("/root/reference" if os.path.isdir("/root/reference") else "")
+    if ref:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", "REF=" + ref], check=False, stdout=subprocess.DEVNULL,
+                       stderr=subprocess.DEVNULL)
 
 
 def lib():
@@ -68,6 +70,7 @@ def lib():
         L.orc_km_oror.argtypes = [i32, i64, i32, P, f64, P, i32]
         L.orc_km_forgy.argtypes = [i32, i64, i32, P, P]
         L.orc_em_sweep_blas.argtypes = [i32, i64, i32, P, P, P, P, P, i32, P, P, P]
+        L.orc_em_sweeps_blas.argtypes = [i32, i64, i32, P, P, P, P, i32, i32, f64, P, P, i32, P, P, P]
         _LIB = L
     return _LIB
 
@@ -257,3 +260,64 @@ def em_sweep_blas(X, pi, mu, sigma, nthreads=0):
     if st != ORC_OK:
         raise RuntimeError("orc_em_sweep_blas failed with status %d" % st)
     return ll.value, pi, mu, sigma
+
+
+def em_sweeps_blas(X, pi, mu, sigma, sweeps, nthreads=0, svd=False, abort_thr=1e5):
+    """`sweeps` FP64 sweeps in one call, organised like SimpleMatrixEM with
+    OpenBLAS level-3 calls, buffers sized once as TrainNoCopy has them, with
+    the condition-number check after each sweep when `svd`
+    (orc_em_sweeps_blas).  Returns (logL per sweep, seconds per sweep, pi, mu,
+    sigma)."""
+    blas = openblas()
+    if blas is None:
+        raise RuntimeError("scipy's bundled OpenBLAS was not found")
+    X = _f32(X)
+    n, d = X.shape
+    pi = np.array(pi, dtype=np.float64, copy=True)
+    mu = np.array(mu, dtype=np.float64, copy=True, order="C")
+    sigma = np.array(sigma, dtype=np.float64, copy=True, order="C")
+    ll = np.full(sweeps, np.nan)
+    sec = np.full(sweeps, np.nan)
+    st = lib().orc_em_sweeps_blas(d, n, len(pi), _p(X), _p(pi), _p(mu), _p(sigma), int(sweeps), int(bool(svd)),
+                                  float(abort_thr), _p(ll), _p(sec), int(nthreads),
+                                  *[ctypes.c_void_p(f) for f in blas[1]])
+    if st != ORC_OK:
+        raise RuntimeError("orc_em_sweeps_blas failed with status %d" % st)
+    return ll, sec, pi, mu, sigma
+
+
+REF_KMEANS = os.path.join(_HERE, "_ref", "ref_kmeans")
+
+
+def ref_kmeans(X, centroids, iterations, seed, nthreads=1):
+    """Run the reference's own NaiveKMA (oracle/_ref/ref_kmeans, built from the
+    reference's sources by `make -C oracle ref`) for `iterations`
+    ComputeMSEAndCorrect calls from `centroids`, its generator seeded with
+    `seed` (SRand, used by CentroidRandomRepair).  Returns (fits, labels per
+    iteration, centroids after each iteration); None when the binary was not
+    built."""
+    import tempfile
+    if not os.path.exists(REF_KMEANS):
+        return None
+    from fastem_gb300 import formats
+    X = _f32(X)
+    C = np.ascontiguousarray(centroids, dtype=np.float64)
+    with tempfile.TemporaryDirectory() as d:
+        formats.write_bin(os.path.join(d, "x.bin"), X)
+        C.tofile(os.path.join(d, "c.f64"))
+        env = dict(os.environ, OMP_NUM_THREADS=str(int(nthreads)))
+        subprocess.run([REF_KMEANS, os.path.join(d, "x.bin"), os.path.join(d, "c.f64"), str(int(iterations)),
+                        str(int(seed)), os.path.join(d, "o.bin")], check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+        b = open(os.path.join(d, "o.bin"), "rb").read()
+    it, n, k, dd = (int(v) for v in np.frombuffer(b[:16], dtype=np.int32))
+    fits, labels, cents = [], [], []
+    off = 16
+    for _ in range(it):
+        fits.append(float(np.frombuffer(b[off:off + 8], dtype=np.float64)[0]))
+        off += 8
+        labels.append(np.frombuffer(b[off:off + 4 * n], dtype=np.int32).copy())
+        off += 4 * n
+        cents.append(np.frombuffer(b[off:off + 8 * k * dd], dtype=np.float64).reshape(k, dd).copy())
+        off += 8 * k * dd
+    return np.array(fits), np.array(labels), np.array(cents)

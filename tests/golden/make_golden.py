@@ -1,8 +1,12 @@
-"""Generate the golden fixtures of tests/golden/ from the FP64 oracle.
+"""Generate the golden fixtures of tests/golden/ from the FP64 oracle, and
+km_ref.npz from the reference itself.
 
-Every fixture is produced by oracle/fem_oracle.cpp on one thread and checked
-against the independent numpy statement in tests/npref.py before it is
-written.  The inputs are stored in the fixture, so it does not depend on the
+Every oracle fixture is produced by oracle/fem_oracle.cpp on one thread and
+checked against the independent numpy statement in tests/npref.py before it
+is written.  km_ref.npz is written by the reference's own NaiveKMA
+(oracle/_ref/ref_kmeans, built from the reference's sources by
+`make -C oracle ref`; skipped when that binary is absent) and checked against
+the oracle before it is written.  The inputs are stored in the fixture, so it does not depend on the
 numpy version that generated them.
 
     python tests/golden/make_golden.py
@@ -69,6 +73,28 @@ def km_ties_fixture():
                         counts=cnt, C1=C1)
 
 
+def km_ref_fixture():
+    # d = 32 (the tensor-core assignment's shape), overlapping blobs so that
+    # many rows are near ties, and one centroid far from every row so that the
+    # first iteration repairs an empty cluster with the generator (seed 17)
+    X, _ = synth.kmeans_blobs(seed=31, n=8192, d=32, k=31, spread=2.5)
+    C0 = np.vstack([X[::256][:31].astype(np.float64), np.full((1, 32), 1e3)])
+    seed, iters = 17, 5
+    out = O.ref_kmeans(X, C0, iters, seed, nthreads=1)
+    if out is None:
+        print("oracle/_ref/ref_kmeans not built: km_ref.npz not written")
+        return
+    fits, labels, cents = out
+    O.rng_seed(seed)
+    C = C0.copy()
+    for i in range(iters):
+        fit, C, cnt, lab = O.km_iterate(X, C, repair=True, nthreads=1)
+        assert (lab == labels[i]).all() and np.allclose(C, cents[i], rtol=1e-13, atol=1e-13)
+        assert abs(fit - fits[i]) <= 1e-13 * fits[i]
+    np.savez_compressed(os.path.join(HERE, "km_ref.npz"), X=X, C0=C0, seed=seed, labels=labels, fits=fits,
+                        centroids=cents)
+
+
 def rng_fixture():
     O.rng_seed(42)
     u42 = np.array([O.rng_uniform() for _ in range(8)])
@@ -80,5 +106,6 @@ if __name__ == "__main__":
     em_fixture()
     km_fixture()
     km_ties_fixture()
+    km_ref_fixture()
     rng_fixture()
     print("golden fixtures written to", HERE)

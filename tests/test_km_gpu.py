@@ -60,6 +60,28 @@ def test_km_golden_fixture(gpu_lib, precision):
             np.testing.assert_allclose(C, z["centroids"][it], rtol=1e-14, atol=1e-14)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_km_matches_reference_fixture(gpu_lib, precision):
+    """Against tests/golden/km_ref.npz, written by the reference's own
+    NaiveKMA::ComputeMSEAndCorrect (Clust/KMAlgorithm.cpp:205-255, built from
+    its sources): d = 32 overlapping blobs with many near ties and an empty
+    cluster repaired from the generator (CentroidRandomRepair, seed 17) in the
+    first iteration.  Labels bit-exact, centroids and fit within FP64
+    summation order."""
+    z = np.load(os.path.join(GOLDEN, "km_ref.npz"))
+    X, C = z["X"], z["C0"].copy()
+    n, d = X.shape
+    with CudaKMA(d, n, C.shape[0], precision=precision, seed=int(z["seed"]), repair=True) as km:
+        km.SetDataset(X)
+        for it in range(len(z["fits"])):
+            fit = km.ComputeMSEAndCorrect(C)
+            lab = km.Assignment()
+            assert np.array_equal(lab, z["labels"][it]), "iteration %d: %d labels differ" % (
+                it, (lab != z["labels"][it]).sum())
+            np.testing.assert_allclose(C, z["centroids"][it], rtol=1e-13, atol=1e-13)
+            assert abs(fit - z["fits"][it]) <= 1e-12 * z["fits"][it]
+
+
 def test_km_exact_ties_lowest_index(gpu_lib):
     z = np.load(os.path.join(GOLDEN, "km_ties.npz"))
     C = z["C0"].copy()

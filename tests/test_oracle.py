@@ -48,6 +48,65 @@ def test_rng_matches_reference_rand(oracle, seed):
     assert got_i == ref_i
 
 
+def _ref_kmeans_or_skip(oracle, *args, **kw):
+    try:
+        out = oracle.ref_kmeans(*args, **kw)
+    except OSError as e:                       # built for another CPU architecture
+        pytest.skip(str(e))
+    if out is None:
+        pytest.skip("oracle/_ref/ref_kmeans not built (reference sources absent)")
+    return out
+
+
+def _oracle_iterations(oracle, X, C0, iters, seed):
+    oracle.rng_seed(seed)
+    C = C0.copy()
+    fits, labels, cents = [], [], []
+    for _ in range(iters):
+        fit, C, _, lab = oracle.km_iterate(X, C, repair=True, nthreads=1)
+        fits.append(fit)
+        labels.append(lab)
+        cents.append(C.copy())
+    return np.array(fits), np.array(labels), np.array(cents)
+
+
+def _km_pin_cases():
+    z = np.load(os.path.join(GOLDEN, "km_blobs.npz"))
+    yield "km_blobs golden", z["X"], z["C0"], 6
+    t = np.load(os.path.join(GOLDEN, "km_ties.npz"))
+    yield "km_ties golden", t["X"], t["C0"], 2
+    X, _ = synth.kmeans_blobs(seed=6, n=1000, d=4, k=3)
+    yield "empty cluster (random repair)", X, np.vstack([X[:3].astype(np.float64), np.full((1, 4), 1e6)]), 3
+    X, _ = synth.kmeans_blobs(seed=21, n=6000, d=32, k=24, spread=1.0)
+    yield "d = 32 blobs, overlapping", X, X[::250][:24].astype(np.float64), 5
+
+
+@pytest.mark.parametrize("threads", [1, 4])
+def test_kmeans_matches_reference_naive_kma(oracle, threads):
+    """The oracle's Lloyd iteration against the reference's own
+    NaiveKMA::ComputeMSEAndCorrect (Clust/KMAlgorithm.cpp:205-255, compiled
+    in place into oracle/_ref with CentroidVector, OpenMPKMAReducer and
+    CentroidRandomRepair): labels and repair draws bit-exact, centroids and fit
+    equal up to the order of the reference's per-thread sums."""
+    for name, X, C0, iters in _km_pin_cases():
+        rf, rl, rc = _ref_kmeans_or_skip(oracle, X, C0, iters, seed=17, nthreads=threads)
+        of, ol, oc = _oracle_iterations(oracle, X, C0, iters, seed=17)
+        assert np.array_equal(rl, ol), name
+        np.testing.assert_allclose(oc, rc, rtol=1e-13, atol=1e-13, err_msg=name)
+        np.testing.assert_allclose(of, rf, rtol=1e-13, err_msg=name)
+
+
+def test_kmeans_golden_made_by_reference(oracle):
+    """tests/golden/km_ref.npz was written by the reference's own NaiveKMA
+    (tests/golden/make_golden.py); where the reference binary is built, it
+    still gives those bytes."""
+    z = np.load(os.path.join(GOLDEN, "km_ref.npz"))
+    rf, rl, rc = _ref_kmeans_or_skip(oracle, z["X"], z["C0"], len(z["fits"]), seed=int(z["seed"]), nthreads=1)
+    assert np.array_equal(rl, z["labels"])
+    np.testing.assert_allclose(rc, z["centroids"], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(rf, z["fits"], rtol=1e-13)
+
+
 def test_rng_golden(oracle):
     z = np.load(os.path.join(GOLDEN, "rng.npz"))
     oracle.rng_seed(42)
@@ -202,3 +261,19 @@ def test_blas_sweep_matches_oracle(oracle):
     np.testing.assert_allclose(pi2, ref["pi"], rtol=1e-11)
     np.testing.assert_allclose(mu2, ref["mu"], rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(sg2, ref["sigma"], rtol=1e-9, atol=1e-12)
+
+
+def test_blas_sweeps_match_oracle_train(oracle):
+    """Several sweeps in one call (buffers sized once, as the reference arm
+    times them) follow the scalar oracle's TrainNoCopy trace."""
+    if oracle.openblas() is None:
+        pytest.skip("scipy's bundled OpenBLAS not found")
+    from fastem_gb300 import synth
+    X, _ = synth.em_large(seed=3, n=5000, d=16, k=6)
+    pi, mu, sg = synth.dsquared_init(X, 6, seed=5)
+    ll, sec, pi2, mu2, sg2 = oracle.em_sweeps_blas(X, pi, mu, sg, 4, nthreads=2)
+    ref = oracle.em_train(X, pi, mu, sg, 4, eps=0.0)
+    assert len(ref["logl"]) == 4 and np.all(sec > 0)
+    np.testing.assert_allclose(ll, ref["logl"], rtol=1e-10)
+    np.testing.assert_allclose(pi2, ref["pi"], rtol=1e-9)
+    np.testing.assert_allclose(sg2, ref["sigma"], rtol=1e-7, atol=1e-10)
