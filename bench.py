@@ -35,6 +35,8 @@ UNIT = "iter/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 PROFILE_FILE = os.path.join(ROOT, "profiles", "em_sweep_n8m_d64_k128.md")
 FALLBACK_TFLOPS = 1900.0  # GB300 bf16 dense burst, used only without measured peaks
+PRECISION_NOTE = ("fp16x3 E-step / fp16 M-step (exact diagonal) tensor cores, fp32 accumulate, "
+                  "fp64 factorisation, logdet and logL")
 
 
 def parse():
@@ -51,6 +53,10 @@ def parse():
     ap.add_argument("--no-fp32", action="store_true", help="skip the FP32 CUDA-core comparison")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--acc-sweeps", type=int, default=20,
+                    help="EM workload: sweeps of the accuracy check against the FP64 GPU path (0 = skip)")
+    ap.add_argument("--no-svd", action="store_true",
+                    help="EM workload: leave out the per-sweep condition-number check (the reference's -S)")
     return ap.parse_args()
 
 
@@ -166,17 +172,18 @@ def em_flops(n, d, k):
     return dict(estep=tri, cov=tri, mstep=tri + 2 * n * k * d, total=2 * tri + 2 * n * k * d)
 
 
-def time_device_sweeps(em, G, warmup, steps, dist, reg=0.0):
+def time_device_sweeps(em, G, warmup, steps, dist, reg=0.0, svd=False):
     """Warm-up sweeps, then `steps` sweeps timed by CUDA events on the
-    library's stream (max over ranks)."""
+    library's stream (max over ranks).  With `svd` every sweep ends with the
+    condition-number check (the reference's default, EM2/EMArgs.cpp:40)."""
     import torch
     em.SetParameters(warmup, 0.0, 1e5, reg)
-    em.TrainNoCopy(G)
+    em.TrainNoCopy(G, svd=svd)
     dist.barrier()
     torch.cuda.synchronize()
     em.TimingReset(True)
     em.SetParameters(steps, 0.0, 1e5, reg)
-    em.TrainNoCopy(G)
+    em.TrainNoCopy(G, svd=svd)
     torch.cuda.synchronize()
     dist.barrier()
     t = em.Timing()
@@ -201,40 +208,103 @@ def cpu_sweep_seconds(X, init, sample, threads):
     return time.perf_counter() - t0, "FP64, OpenMP scalar loops"
 
 
+def cpu_full_sweeps(X, init, burn_in, timed, threads, svd):
+    """`burn_in` + `timed` FP64 sweeps of the oracle over ALL rows in one call
+    (buffers sized once, as EMAlgorithm::TrainNoCopy runs its sweeps),
+    organised like the reference's SimpleMatrixEM: OpenMP over row blocks,
+    single-threaded OpenBLAS dtrmm / dgemm / dsyrk inside each thread where the
+    reference calls MKL; with `svd` the condition-number check after each
+    sweep.  Returns (seconds of each timed sweep, logL trace, how)."""
+    from oracle import oracle as O
+    O.lib()
+    if O.openblas() is None:
+        raise RuntimeError("scipy's bundled OpenBLAS was not found: no CPU baseline")
+    O.em_sweeps_blas(X[:4096], *init, 1, nthreads=threads)    # load the libraries, start the thread pool
+    ll, sec, *_ = O.em_sweeps_blas(X, *init, burn_in + timed, nthreads=threads, svd=svd)
+    how = "FP64, OpenMP + OpenBLAS dtrmm/dgemm/dsyrk" + (", condition check each sweep" if svd else "")
+    return sec[burn_in:], ll, how
+
+
+def em_config(n, d, k, world, svd):
+    return {"workload": "em_large N=%d d=%d K=%d, one EM sweep per step" % (n, d, k),
+            "n": n, "d": d, "k": k, "parallelism": "replicas" if world > 1 else "single",
+            "svd": "off (-S)" if not svd else "on (the reference default: condition number of every "
+                                               "covariance after each sweep, abort above 1e5)",
+            "l2": "inputs larger than L2 (X 2.1 GB fp32 + 2.1 GB fp16 splits, posteriors 4.3 GB)"}
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's CPU algorithm (the oracle's FP64
     restatement of SimpleMatrixEM, OpenMP with OpenBLAS level-3 calls where
-    the reference calls MKL, all host cores) on a bounded row sample per step;
-    the reference itself cannot be compiled here (Eigen 3.4, MKL, libnuma and
-    MPI are absent)."""
+    the reference calls MKL, all host cores) sweeping ALL N rows: `warmup`
+    untimed sweeps, then `steps` timed sweeps, in one TrainNoCopy-like call.
+    The reference itself cannot be compiled here (Eigen 3.4, MKL, libnuma and
+    MPI are absent).  With svd on (the reference's default) every sweep ends
+    with the condition check, as the GPU arm's sweeps do."""
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
     n, d, k = args.n, 64, args.k
-    sample = 1 << 16
     X, init = workload(n, k)
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_sweep_seconds(X, init, sample, threads)
-    tot = 0.0
-    for _ in range(args.steps):
-        dt, how = cpu_sweep_seconds(X, init, sample, threads)
-        tot += dt
-    per_sweep_full = tot / args.steps * (n / sample)
-    value = 1.0 / per_sweep_full
+    t0 = time.perf_counter()
+    sec, ll, how = cpu_full_sweeps(X, init, args.warmup, args.steps, threads, not args.no_svd)
+    wall = time.perf_counter() - t0
+    per_sweep = float(np.mean(sec))
+    value = 1.0 / per_sweep
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep_full * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic em_large (seeded)",
-        "config": {"workload": "em_large N=%d d=%d K=%d, one EM sweep per step" % (n, d, k)},
+        "data": "synthetic em_large (seeded; Dirichlet(2) weights, N(0,25I) means, Haar-rotated "
+                "covariances with eigenvalues log-uniform in [0.1,10])",
+        "config": em_config(n, d, k, world, not args.no_svd),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "1 sweep (%s) over the first %d of %d rows per step, scaled x%d"
-                                   % (how, sample, n, n // sample)},
+                         "how": "%s, %d warm-up + %d timed sweeps over all %d rows" % (how, args.warmup,
+                                                                                     args.steps, n),
+                         "sweep_seconds": [round(float(x), 3) for x in sec], "wall_s": wall},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def accuracy_vs_fp64(X, init, sweeps, local):
+    """The metric's |dlogL/N| <= 1e-5 clause, measured: `sweeps` sweeps from
+    the same initial mixture through the FP64 GPU path (the parity path,
+    equal to the oracle within 1e-10 over 50 sweeps in the tests), the mixed
+    path and the FP32 path.  Per sweep |L - L_fp64| / N (the pre-M-step logL
+    each sweep returns, EM2/EMAlgorithm.cpp:170-178), and the final mixture's
+    largest differences from the FP64 one."""
+    from fastem_gb300 import CudaMatrixEM, GaussianMixture
+    n, d = X.shape
+    k = len(init[0])
+    tr, mix, secs = {}, {}, {}
+    for prec in ("fp64", "mixed", "fp32"):
+        with CudaMatrixEM(d, n, k, precision=prec, device=local) as em:
+            em.CopyDataset(X)
+            em.SetParameters(sweeps, 0.0, 1e12)
+            G = GaussianMixture(*init)
+            t0 = time.perf_counter()
+            em.TrainNoCopy(G)
+            secs[prec] = time.perf_counter() - t0
+            tr[prec], mix[prec] = em.logl_trace.copy(), G
+    out = {"vs": "fp64 GPU path (oracle-pinned)", "sweeps": sweeps, "n": n, "bound": 1e-5,
+           "fp64_seconds": secs["fp64"]}
+    ref = tr["fp64"]
+    for prec in ("mixed", "fp32"):
+        m = min(len(ref), len(tr[prec]))
+        per = np.abs(tr[prec][:m] - ref[:m]) / n
+        G, R = mix[prec], mix["fp64"]
+        cov_rel = max(float(np.linalg.norm(G.covs[j] - R.covs[j]) / np.linalg.norm(R.covs[j]))
+                      for j in range(k))
+        out[prec] = {"max_dlogL_per_N": float(per.max()), "final_dlogL_per_N": float(per[-1]),
+                     "per_sweep": [float("%.3g" % v) for v in per],
+                     "within_bound": bool(per.max() <= 1e-5),
+                     "final_max_dweight": float(np.max(np.abs(G.weights - R.weights))),
+                     "final_max_dmean": float(np.max(np.abs(G.means - R.means))),
+                     "final_max_cov_rel_frobenius": cov_rel}
+    return out
 
 
 def main():
@@ -268,12 +338,13 @@ def main():
     fl = em_flops(n, d, k)
 
     # ---- mixed precision, inputs resident in HBM
+    svd = not args.no_svd
     em = CudaMatrixEM(d, n, k, precision="mixed", device=local)
     em.CopyDataset(X)
     G = GaussianMixture(*init)
     clocks = Clocks(local)
     clocks.start()
-    t = time_device_sweeps(em, G, args.warmup, args.steps, dist)
+    t = time_device_sweeps(em, G, args.warmup, args.steps, dist, svd=svd)
     clk = clocks.stop()
     train_ms = dist.max(t["train_ms"])
     sweeps = t["sweeps"]
@@ -299,6 +370,8 @@ def main():
             "frac": achieved / peak, "peak_source": peak_src, "traffic": profiled_traffic(kern),
             "algorithmic_flops_per_launch": dom_flops, "launch_ms": dom_ms,
             "estep_ms": est_ms, "mstep_ms": mst_ms, "cov_ms": cov_ms, "factor_ms": fac_ms,
+            "estep_frac": fl["estep"] / (est_ms / 1e3) / 1e12 / peak,
+            "cov_frac": fl["cov"] / (cov_ms / 1e3) / 1e12 / peak,
             "sweep_algorithmic_tflops": fl["total"] / (ms_step / 1e3) / 1e12}
 
     # ---- end to end through the C-ABI with pinned host buffers
@@ -313,7 +386,7 @@ def main():
         for _ in range(steps):
             from fastem_gb300 import _capi as C
             C.check(C.lib().fem_em_upload(em.handle, ctypes.c_void_p(hostX.data_ptr()), d))
-            em.TrainNoCopy(Ge)          # uploads the mixture, 1 sweep, reads it back
+            em.TrainNoCopy(Ge, svd=svd)  # uploads the mixture, 1 sweep, reads it back
         dt = dist.max(time.perf_counter() - t0)
         pbytes = k * (1 + d + d * d) * 8
         e2e = {"value": world * steps / dt, "unit": UNIT, "h2d_bytes_per_step": n * d * 4 + pbytes,
@@ -328,21 +401,30 @@ def main():
         e32.CopyDataset(X)
         G32 = GaussianMixture(*init)
         s32 = max(2, args.steps // 3)
-        t32 = time_device_sweeps(e32, G32, max(1, min(args.warmup, 2)), s32, dist)
+        t32 = time_device_sweeps(e32, G32, max(1, min(args.warmup, 2)), s32, dist, svd=svd)
         ms32 = dist.max(t32["train_ms"]) / t32["sweeps"]
         fp32 = {"value": world * 1e3 / ms32, "ms_per_step": ms32, "steps": t32["sweeps"],
-                "estep_ms": t32["estep_ms"] / t32["sweeps"], "mstep_ms": t32["mstep_ms"] / t32["sweeps"]}
+                "estep_ms": t32["estep_ms"] / t32["sweeps"], "mstep_ms": t32["mstep_ms"] / t32["sweeps"],
+                "cov_ms": t32["cov_ms"] / t32["sweeps"],
+                "estep_fp32_frac": fl["estep"] / (t32["estep_ms"] / t32["sweeps"] / 1e3) / 1e12
+                / (152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12),
+                "mstep_fp32_frac": fl["mstep"] / (t32["mstep_ms"] / t32["sweeps"] / 1e3) / 1e12
+                / (152 * 128 * 2 * (clk.get("sm_mhz") or 2070.0) * 1e6 / 1e12),
+                "fp32_peak_note": "fractions of the nominal FP32 CUDA-core rate (152 SMs x 128 lanes x 2 flop "
+                                  "at the sampled SM clock)"}
         e32.close()
 
-    # ---- CPU baseline: the oracle port on a bounded sample (rank 0)
+    # ---- the metric's accuracy clause, outside the timed region
+    acc = accuracy_vs_fp64(X, init, args.acc_sweeps, local) if args.acc_sweeps > 0 else None
+
+    # ---- CPU baseline: the oracle port, 1 burn-in + 2 timed sweeps over all rows (rank 0)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        sample = 1 << 16
         threads = os.cpu_count() or 1
-        cpu_sweep_seconds(X, init, 1 << 12, threads)   # warm the library
-        dt, how = cpu_sweep_seconds(X, init, sample, threads)
-        cpu = {"value": 1.0 / (dt * n / sample), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "1 sweep (%s) over the first %d of %d rows, scaled x%d" % (how, sample, n, n // sample)}
+        sec, _, how = cpu_full_sweeps(X, init, 1, 2, threads, svd)
+        cpu = {"value": 1.0 / float(np.mean(sec)), "unit": UNIT, "cores": threads, "kind": "port",
+               "how": "%s, 1 burn-in + 2 timed sweeps over all %d rows" % (how, n),
+               "sweep_seconds": [round(float(x), 3) for x in sec]}
 
     dist.close()
     if rank != 0:
@@ -351,13 +433,11 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": sweeps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp16",
-        "precision": "fp16x3 E-step / fp16 M-step (exact diagonal) tensor cores, fp32 accumulate, "
-                     "fp64 factorisation, logdet and logL",
+        "precision": PRECISION_NOTE,
         "data": "synthetic em_large (seeded; Dirichlet(2) weights, N(0,25I) means, Haar-rotated "
                 "covariances with eigenvalues log-uniform in [0.1,10])",
-        "config": {"workload": "em_large N=%d d=%d K=%d, one EM sweep per step" % (n, d, k),
-                   "n": n, "d": d, "k": k, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (X 2.1 GB fp32 + 2.1 GB fp16 splits, posteriors 4.3 GB)"},
+        "config": em_config(n, d, k, world, svd),
+        "accuracy": acc,
         "roofline": roof, "e2e": e2e, "fp32_plain": fp32,
         "speedup_vs_fp32_plain": (value / fp32["value"]) if fp32 else None,
         "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
