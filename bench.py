@@ -389,8 +389,17 @@ def main():
             em.TrainNoCopy(Ge, svd=svd)  # uploads the mixture, 1 sweep, reads it back
         dt = dist.max(time.perf_counter() - t0)
         pbytes = k * (1 + d + d * d) * 8
+        # where an end-to-end step goes: the upload alone, the train call alone
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            C.check(C.lib().fem_em_upload(em.handle, ctypes.c_void_p(hostX.data_ptr()), d))
+        up = (time.perf_counter() - t0) / steps
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            em.TrainNoCopy(Ge, svd=svd)
+        tr = (time.perf_counter() - t0) / steps
         e2e = {"value": world * steps / dt, "unit": UNIT, "h2d_bytes_per_step": n * d * 4 + pbytes,
-               "d2h_bytes_per_step": pbytes + 8 + 16}
+               "d2h_bytes_per_step": pbytes + 8 + 16, "upload_ms": up * 1e3, "train_call_ms": tr * 1e3}
         del hostX
     em.close()
 

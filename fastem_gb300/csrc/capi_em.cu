@@ -97,6 +97,21 @@ int enqueue_mstep(fem_em *h) {
 
 int max_cond(fem_em *h, double *cond) { return em_max_cond(h, cond); }
 
+// The condition test of TrainNoCopy (EM2/EMAlgorithm.cpp:147-151,157-161):
+// the factorisation just synchronised left max_j ||Sigma_j||_F ||L_j^-1||_F^2,
+// an upper bound of every cond(Sigma_j), in the status word.  When that bound
+// is within AbortThr no condition number can exceed it, and *cond receives the
+// bound; otherwise the exact eigenvalues are computed (k_cond_jacobi) and
+// *cond is the largest condition number, as FindLargestConditionNumber.
+int cond_check(fem_em *h, double *cond) {
+  const double b = h->hstat->cond_bound * (1.0 + 1e-12);
+  if (b > 0.0 && b <= h->cfg.abort_thr) {
+    *cond = b;
+    return FEM_OK;
+  }
+  return max_cond(h, cond);
+}
+
 void free_all(fem_em *h) {
   if (h->tc) em_tc_destroy(h);
   dfree(h->X);
@@ -261,8 +276,11 @@ static int upload_common(fem_em *h, const float *X, int64_t ld, cudaMemcpyKind k
     return FEM_ERR_BAD_ARG;
   }
   FEM_CUDA(cudaSetDevice(h->cfg.device));
-  FEM_CUDA(cudaMemcpy2DAsync(h->X, (size_t)h->d * sizeof(float), X, (size_t)ld * sizeof(float),
-                             (size_t)h->d * sizeof(float), (size_t)h->n, kind, h->stream));
+  if (ld == h->d)   // contiguous rows: one linear copy
+    FEM_CUDA(cudaMemcpyAsync(h->X, X, (size_t)h->n * h->d * sizeof(float), kind, h->stream));
+  else
+    FEM_CUDA(cudaMemcpy2DAsync(h->X, (size_t)h->d * sizeof(float), X, (size_t)ld * sizeof(float),
+                               (size_t)h->d * sizeof(float), (size_t)h->n, kind, h->stream));
   if (mixed(h)) FEM_TRY(em_tc_upload(h));
   FEM_CUDA(cudaStreamSynchronize(h->stream));
   h->have_data = true;
@@ -376,7 +394,7 @@ int fem_em_train(fem_em *h, int svd, double *logl_trace, double *e_trace, int ca
   }
   double cond = 0.0;
   if (svd) {
-    FEM_TRY(max_cond(h, &cond));
+    FEM_TRY(cond_check(h, &cond));
     if (cond > h->cfg.abort_thr) {
       set_error("Condition number of a covariance matrix is too high (%g)", cond);
       return FEM_ERR_COND_ABORT;
@@ -398,7 +416,7 @@ int fem_em_train(fem_em *h, int svd, double *logl_trace, double *e_trace, int ca
       return st;
     }
     if (svd) {
-      FEM_TRY(max_cond(h, &cond));
+      FEM_TRY(cond_check(h, &cond));
       if (cond > h->cfg.abort_thr) {
         if (iter_counter) *iter_counter = it;
         set_error("Condition number of a covariance matrix is too high (%g)", cond);

@@ -111,6 +111,39 @@ __device__ inline double block_chol_logdet(const double *A, int d) {
   return v;
 }
 
+// An upper bound of the condition number lambda_max / lambda_min of the
+// positive definite sym(lower(S)) = L L^T, from norms only:
+//   lambda_max <= ||Sigma||_F and 1 / lambda_min = ||L^-1||_2^2 <= ||L^-1||_F^2.
+// S is row-major (its lower triangle is used), Wi = L^-1 (lower).  At most
+// d^1.5 times the true value; the caller runs the exact eigenvalues
+// (block_jacobi_cond) only when the bound does not settle a test.  Sums in a
+// fixed order; the value in every thread.  blockDim.x <= 256.
+__device__ inline double block_cond_bound(const double *S, const double *Wi, int d) {
+  __shared__ double red_s[256], red_w[256];
+  __shared__ double s_b;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double fs = 0.0, fw = 0.0;
+  for (int e = tid; e < d * d; e += nt) {
+    const int r = e / d, c = e - r * d;
+    if (c > r) continue;
+    const double v = S[e], w = Wi[e];
+    fs += (c == r ? 1.0 : 2.0) * v * v;
+    fw += w * w;
+  }
+  red_s[tid] = fs;
+  red_w[tid] = fw;
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0.0, b = 0.0;
+    for (int t = 0; t < nt; t++) a += red_s[t], b += red_w[t];
+    s_b = sqrt(a) * b;
+  }
+  __syncthreads();
+  const double v = s_b;
+  __syncthreads();
+  return v;
+}
+
 // NormalDensity::ComputeConditionNumber (EM2/NormalDensity.cpp:67-71): the
 // eigenvalues of the symmetric matrix in A (overwritten) by cyclic Jacobi in
 // FP64.  Each sweep runs the n - 1 rounds of a round-robin schedule; a round

@@ -551,7 +551,8 @@ __global__ void k_final_cov(const double *__restrict__ part, int chunks, int K, 
 // EM2/MatrixEM.cpp:83-87) in FP64, one CTA per component: symmetric copy of
 // the lower triangle, right-looking Cholesky (a pivot <= 0 fails, as in
 // Eigen's LLT), log det = 2 sum log L_ii, W = L^-1 by column substitution,
-// log coefficient log pi_j - d/2 log 2pi - 1/2 log det.
+// log coefficient log pi_j - d/2 log 2pi - 1/2 log det, and an upper bound
+// of the condition number (block_cond_bound) folded into st->cond_bound.
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_factor(int K, int d, double reg, int regularize, double *__restrict__ sigma,
@@ -569,7 +570,10 @@ k_factor(int K, int d, double reg, int regularize, double *__restrict__ sigma,
   }
   block_lower_inverse(A, d, Wi);
   const double ld = block_chol_logdet(A, d);
+  const double cb = block_cond_bound(S, Wi, d);
   if (tid == 0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(&st->cond_bound), (unsigned long long)__double_as_longlong(cb));
     logdet[j] = ld;
     const double lc = log(pi[j]) - 0.5 * (double)d * log(2.0 * M_PI) - 0.5 * ld;
     logc[j] = lc;

@@ -130,6 +130,7 @@ struct TcEmPlan {
   float *chi = nullptr;                 // float(log coefficient); -inf for padding components
   float *X64 = nullptr;                 // n x 64 zero-padded FP32 rows when d < 64
   int *err = nullptr;                   // device status of the bounded waits
+  float *amax = nullptr;                // upload: largest |x| (FP16 range check)
   int egrid = 0, mgrid = 0, cgx = 0, cgy = 0;
   int kp = 0, d = 0;                    // components padded to a multiple of 4; true dimension
 };
@@ -946,6 +947,7 @@ int em_tc_create(fem_em *h) {
   if (h->d < kD) FEM_TRY(dalloc(&p->X64, (size_t)n * kD));
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
+  FEM_TRY(dalloc(&p->amax, 1));
   const int64_t npairs = ((n + kTileM - 1) / kTileM + 1) / 2;
   p->egrid = (int)std::min<int64_t>(sms, npairs);
   FEM_TRY(dalloc(&p->epart, p->egrid));
@@ -1005,21 +1007,20 @@ void em_tc_destroy(fem_em *h) {
   dfree(p->chi);
   dfree(p->X64);
   dfree(p->err);
+  dfree(p->amax);
   delete p;
   h->tc = nullptr;
 }
 
 int em_tc_upload(fem_em *h) {
   TcEmPlan *p = h->tc;
-  float *amax = nullptr;
-  FEM_TRY(dalloc(&amax, 1));
+  float *amax = p->amax;
   FEM_CUDA(cudaMemsetAsync(amax, 0, sizeof(float), h->stream));
   const int blocks = (int)std::min<int64_t>(4 * sm_count(), (h->n + 63) / 64);
   k_split_x<<<blocks, 256, 0, h->stream>>>(h->X, h->n, h->d, h->Xhi, h->Xlo, p->XhT, p->XlT, p->np, p->X64, amax);
   float m = 0.f;
   cudaMemcpyAsync(&m, amax, sizeof(float), cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
-  dfree(amax);
   if (e != cudaSuccess) {
     set_error("dataset split failed: %s", cudaGetErrorString(e));
     return FEM_ERR_CUDA;

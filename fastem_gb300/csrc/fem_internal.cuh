@@ -84,6 +84,7 @@ struct DevStatus {
   double fit;          // k-means sum of squared distances
   int track_changes;   // k-means: compare each new label with the stored one (set by the host)
   int changed;         // k-means: some label differs from the stored one
+  double cond_bound;   // EM: max over components of ||Sigma_j||_F ||L_j^-1||_F^2 (>= cond(Sigma_j))
 };
 
 // ------------------------------------------------------------------ EM handle

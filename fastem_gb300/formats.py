@@ -1,7 +1,8 @@
 """The reference's file formats, for tests and tooling.
 
   .bin      MultithreadedDataset (Util/MultithreadedDataset.cpp:119-134): int32
-            rows (or -1 then int64 rows), int32 cols, rows of float32
+            rows and int32 cols (or int32 -1, int32 cols, int64 rows), then the
+            rows of float32
   .cmp      GaussianMixture::Write / read (EM2/GaussianMixture.cpp:155-171,
             228-244): int32 K, int32 d, per component the d x d covariance
             (row-major), the mean and the weight as float64, then one float64

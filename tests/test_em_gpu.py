@@ -166,6 +166,37 @@ def test_em_condition_abort(gpu_lib):
         assert em.FindLargestConditionNumber() == pytest.approx(1e6, rel=1e-9)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_condition_abort_threshold_sides(gpu_lib, oracle, precision):
+    """The per-sweep condition test settles most sweeps with the bound
+    ||Sigma||_F ||L^-1||_F^2 and computes the eigenvalues only when the bound
+    exceeds AbortThr: the decision must be the reference's either way.  With
+    AbortThr just above the largest condition number after the first sweep the
+    run continues (the bound is above it, so the exact test decides); just
+    below, it stops at that sweep with ConditionAbort."""
+    n, d, k = 1 << 14, 64, 4
+    X, _ = synth.em_large(seed=3, n=n, d=d, k=k)
+    init = synth.forgy_init(X, k, seed=1)
+    # condition numbers after sweep 1, from the oracle's FP64 sweep
+    r1 = oracle.em_train(X, *init, 1, eps=0.0, abort_thr=1e30)
+    ev = np.linalg.eigvalsh(np.tril(r1["sigma"]) + np.tril(r1["sigma"], -1).transpose(0, 2, 1))
+    c1 = float(np.max(ev.max(axis=1) / ev.min(axis=1)))
+    assert c1 > 1.0                                # the Forgy covariances are identities
+    margin = 1e-6 if precision == "fp64" else 1e-3  # the mixed covariances differ from FP64 in ~1e-6
+    for thr, aborts in ((c1 * (1 + margin), False), (c1 * (1 - margin), True)):
+        with CudaMatrixEM(d, n, k, precision=precision) as em:
+            em.CopyDataset(X)
+            em.SetParameters(1, 0.0, thr)
+            G = GaussianMixture(*init)
+            if aborts:
+                with pytest.raises(C.ConditionAbort):
+                    em.TrainNoCopy(G, svd=True)
+                assert em.GetIterCounter() == 1
+            else:
+                em.TrainNoCopy(G, svd=True)
+                assert em.GetIterCounter() == 2
+
+
 @pytest.mark.parametrize("d,k,precision", [(8, 5, "fp64"), (63, 3, "fp32"), (64, 4, "mixed"), (200, 2, "fp64")])
 def test_condition_number_on_device(gpu_lib, d, k, precision):
     """FindLargestConditionNumber: FP64 Jacobi eigenvalues on the device
