@@ -149,6 +149,12 @@ k_na_classify(const float *__restrict__ X, int64_t n, int K, const float *__rest
       if (lb2 > U) {
         best = na_dist64(cent + (size_t)j1 * D, x, D);
       } else {
+        // candidates within the bound, decided in FP64; a row whose FP32
+        // distances are not finite (NaN, or beyond FP32 range) has no
+        // candidate and is decided over every centroid, so it gets the
+        // reference's answer: label -1 and DBL_MAX where no distance is
+        // below DBL_MAX (a NaN row)
+        lab = -1;
         best = DBL_MAX;
         for (int j = 0; j < K; j++) {
           const float *c = sC + j * D;
@@ -166,6 +172,14 @@ k_na_classify(const float *__restrict__ X, int64_t n, int K, const float *__rest
             }
           }
         }
+        if (lab < 0)
+          for (int j = 0; j < K; j++) {
+            const double s64 = na_dist64(cent + (size_t)j * D, x, D);
+            if (s64 < best) {
+              best = s64;
+              lab = j;
+            }
+          }
       }
       labels[base + tid] = lab;
       fit += best;
@@ -218,12 +232,17 @@ int na_setup(int device, NaDevice *out) {
   int prev = 0;
   FEM_CUDA(cudaGetDevice(&prev));
   if (prev != device) FEM_CUDA(cudaSetDevice(device));
-  void *p = nullptr;
-  cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
   int sms = 0, major = 0, minor = 0;
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaError_t e = cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  if (e == cudaSuccess && (major != 10 || minor != 3)) {
+    if (prev != device) cudaSetDevice(prev);
+    set_error("device %d is sm_%d%d; this library is built for sm_103 (GB300) only", device, major, minor);
+    return FEM_ERR_NO_DEVICE;
+  }
+  void *p = nullptr;
+  if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_na_scratch);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = na_raise_smem<2>();
   if (e == cudaSuccess) e = na_raise_smem<4>();
   if (e == cudaSuccess) e = na_raise_smem<8>();
@@ -234,10 +253,6 @@ int na_setup(int device, NaDevice *out) {
   if (e != cudaSuccess) {
     set_error("k-means classification set-up on device %d failed: %s", device, cudaGetErrorString(e));
     return FEM_ERR_CUDA;
-  }
-  if (major != 10 || minor != 3) {
-    set_error("device %d is sm_%d%d; this library is built for sm_103 (GB300) only", device, major, minor);
-    return FEM_ERR_NO_DEVICE;
   }
   nd.scratch = p;
   nd.sms = sms;
@@ -278,6 +293,15 @@ extern "C" int fem_km_classify_noalloc(int d, int64_t n, int k, const float *dX,
   if (device < 0 || device >= ndev || device >= kNaMaxDevices) {
     set_error("fem_km_classify_noalloc: device %d out of range", device);
     return FEM_ERR_BAD_ARG;
+  }
+  // an error left pending by earlier work of the caller would otherwise be
+  // read back below as this call's launch failure: report it as what it is
+  // (and leave it pending for the caller)
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    set_error("fem_km_classify_noalloc: a CUDA error was already pending before this call: %s",
+              cudaGetErrorString(pending));
+    return FEM_ERR_CUDA;
   }
   NaDevice nd;
   FEM_TRY(na_setup(device, &nd));
