@@ -29,7 +29,7 @@ EXPORTS = [
     "fem_em_config_default", "fem_em_create", "fem_em_destroy", "fem_em_set_parameters",
     "fem_em_upload", "fem_em_upload_device", "fem_em_set_params", "fem_em_get_params",
     "fem_em_train", "fem_em_init_densities", "fem_em_precompute", "fem_em_mstep",
-    "fem_em_max_condition", "fem_em_get_posteriors", "fem_em_retrieve_classes",
+    "fem_em_max_condition", "fem_em_selftest_wait_expiry", "fem_em_get_posteriors", "fem_em_retrieve_classes",
     "fem_em_posterior_correlation",
     "fem_em_get_factors", "fem_em_timing_reset", "fem_em_timing_get", "fem_em_timing_total",
     "fem_em_timing_covariance",
@@ -102,6 +102,7 @@ def lib():
         "fem_em_precompute": ([P, P], i32),
         "fem_em_mstep": ([P], i32),
         "fem_em_max_condition": ([P, P], i32),
+        "fem_em_selftest_wait_expiry": ([P, i64, P], i32),
         "fem_em_get_posteriors": ([P, P], i32),
         "fem_em_retrieve_classes": ([P, P], i32),
         "fem_em_posterior_correlation": ([P, P], i32),

@@ -67,6 +67,7 @@ int reset_status(fem_em *h) {
   s.chol_failed = INT_MAX;
   *h->hstat = s;
   FEM_CUDA(cudaMemcpyAsync(h->dstat, h->hstat, sizeof(DevStatus), cudaMemcpyHostToDevice, h->stream));
+  if (mixed(h) && h->tc) FEM_TRY(em_tc_reset_err(h));
   return FEM_OK;
 }
 
@@ -367,6 +368,23 @@ int fem_em_mstep(fem_em *h) {
   FEM_TRY(reset_status(h));
   FEM_TRY(enqueue_mstep(h));
   h->factored = false;
+  return sync_status(h);
+}
+
+int fem_em_selftest_wait_expiry(fem_em *h, int64_t budget_cycles, int *roles) {
+  FEM_TRY(check_handle(h));
+  if (!mixed(h) || !h->tc) {
+    set_error("the bounded-wait self-test runs on a mixed-precision handle");
+    return FEM_ERR_UNSUPPORTED;
+  }
+  if (!roles || budget_cycles < 1000 || budget_cycles > 4000000000LL) {
+    set_error("self-test budget must be in [1e3, 4e9] cycles");
+    return FEM_ERR_BAD_ARG;
+  }
+  FEM_CUDA(cudaSetDevice(h->cfg.device));
+  FEM_TRY(reset_status(h));
+  FEM_TRY(em_tc_wait_selftest(h, (long long)budget_cycles, roles));
+  h->factored = false;     // TMEM and the status word went through the expiry path
   return sync_status(h);
 }
 

@@ -33,6 +33,11 @@ void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *
 void timing_begin(fem_em *h, int slot);
 int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);
 int em_tc_classes(fem_em *h, int32_t *dcls);
+// clears the mixed kernels' bounded-wait status word
+int em_tc_reset_err(fem_em *h);
+// runs the bounded-wait expiry self-test kernel; *roles = bit mask of the
+// waits that gave up (1 consumer, 2 drain, 4 and 8 the two flag-driven waiters)
+int em_tc_wait_selftest(fem_em *h, long long budget, int *roles);
 
 // host_linalg.cpp
 // largest condition number of the K covariances (FP64 Jacobi on the device)

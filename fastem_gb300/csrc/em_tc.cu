@@ -131,6 +131,7 @@ struct TcEmPlan {
   float *X64 = nullptr;                 // n x 64 zero-padded FP32 rows when d < 64
   int *err = nullptr;                   // device status of the bounded waits
   float *amax = nullptr;                // upload: largest |x| (FP16 range check)
+  int *roles = nullptr;                 // bounded-wait expiry self-test: which waits gave up
   int egrid = 0, mgrid = 0, cgx = 0, cgy = 0;
   int kp = 0, d = 0;                    // components padded to a multiple of 4; true dimension
 };
@@ -783,6 +784,47 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
   }
 }
 
+// ================================================= bounded-wait expiry
+// The exit path every warp-specialised kernel here relies on, run on purpose:
+// one CTA with the roles of those kernels, whose producer never delivers.
+// Warp 1 allocates all 512 TMEM columns (as the E-step and covariance kernels
+// do) and waits for a barrier nothing arrives on, with `budget` cycles: the
+// wait runs out, sets the status word and returns false; its drain wait
+// (which ignores the status word, as the drains before TMEM release do) runs
+// out too.  Warps 2 and 3 wait, off the critical path, for a barrier warp 1
+// would have completed; they leave because the status word is set, not by
+// their own (long) budget.  Every warp then reaches the final barrier and
+// warp 1 releases TMEM.  roles[0..3] record which waits gave up.
+__global__ void __launch_bounds__(128, 1) k_wait_expiry(long long budget, int *err, int *roles) {
+  __shared__ uint64_t full, done;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(&full, 1);
+    mbar_init(&done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(&tslot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    if (mbar_wait_warp(&full, 0, err, budget)) {
+      if (lane == 0) mbar_arrive(&done);
+    } else if (lane == 0) {
+      roles[0] = 1;
+    }
+    if (lane == 0 && !mbar_wait_drain(&full, 0, budget)) roles[1] = 1;
+  } else if (warp >= 2) {
+    if (!mbar_wait_lazy_warp(&done, 0, err, 200) && lane == 0) roles[warp] = 1;
+  }
+  // warp 0, the producer, delivers nothing
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tslot, 512);
+}
+
 // ================================================ operand preparation
 // W = L^-1 (FP64) -> FP16 hi/lo in the permuted row order; b = L^-1 mu;
 // row of (component j, output k) = group j/2, k-block position 3 - k/16,
@@ -948,6 +990,7 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(dalloc(&p->err, 1));
   FEM_CUDA(cudaMemset(p->err, 0, sizeof(int)));
   FEM_TRY(dalloc(&p->amax, 1));
+  FEM_TRY(dalloc(&p->roles, 4));
   const int64_t npairs = ((n + kTileM - 1) / kTileM + 1) / 2;
   p->egrid = (int)std::min<int64_t>(sms, npairs);
   FEM_TRY(dalloc(&p->epart, p->egrid));
@@ -1008,6 +1051,7 @@ void em_tc_destroy(fem_em *h) {
   dfree(p->X64);
   dfree(p->err);
   dfree(p->amax);
+  dfree(p->roles);
   delete p;
   h->tc = nullptr;
 }
@@ -1080,6 +1124,28 @@ int em_tc_mstep(fem_em *h) {
   FEM_CUDA(cudaGetLastError());
   k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
   h->launches += 5;
+  return FEM_OK;
+}
+
+// a wait that ran out in an earlier call leaves the status word set; each new
+// call starts from zero (the context itself stays usable: nothing faulted)
+int em_tc_reset_err(fem_em *h) {
+  FEM_CUDA(cudaMemsetAsync(h->tc->err, 0, sizeof(int), h->stream));
+  return FEM_OK;
+}
+
+int em_tc_wait_selftest(fem_em *h, long long budget, int *roles) {
+  TcEmPlan *p = h->tc;
+  FEM_CUDA(cudaMemsetAsync(p->roles, 0, 4 * sizeof(int), h->stream));
+  k_wait_expiry<<<1, 128, 0, h->stream>>>(budget, p->err, p->roles);
+  FEM_CUDA(cudaGetLastError());
+  k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
+  FEM_CUDA(cudaGetLastError());
+  int r[4] = {0, 0, 0, 0};
+  FEM_CUDA(cudaMemcpyAsync(r, p->roles, sizeof r, cudaMemcpyDeviceToHost, h->stream));
+  FEM_CUDA(cudaStreamSynchronize(h->stream));
+  *roles = (r[0] ? 1 : 0) | (r[1] ? 2 : 0) | (r[2] ? 4 : 0) | (r[3] ? 8 : 0);
+  h->launches += 2;
   return FEM_OK;
 }
 

@@ -1,9 +1,11 @@
 // tc_ptx.cuh -- inline-PTX building blocks for sm_103a: mbarriers, TMA
 // (cp.async.bulk.tensor), tcgen05 MMA / TMEM allocation / TMEM loads.
 //
-// Every wait is bounded by a clock budget: a wait that runs out records
-// `kErrTimeout` in the kernel's status word and returns false, so callers
-// leave their loops and the CTA still releases its TMEM and exits.
+// Every wait is bounded by a clock budget (kWaitBudgetCycles unless a caller
+// passes a shorter one): a wait that runs out sets the kernel's status word
+// and returns false, so callers leave their loops and the CTA still releases
+// its TMEM and exits; the other roles' waits see the status word and leave
+// too.
 #pragma once
 
 #include <cuda.h>
@@ -72,7 +74,8 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parit
 
 // bounded wait for the phase with the given parity to complete; the error
 // flag and the clock budget are checked every 64 tries
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
+                                          long long budget = kWaitBudgetCycles) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
@@ -81,7 +84,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
     for (int i = 0; i < 64; i++)
       if (mbar_try_wait(a, parity)) return true;
     if (*(volatile int *)err) return false;
-    if (clock64() - t0 > kWaitBudgetCycles) {
+    if (clock64() - t0 > budget) {
       atomicExch(err, 1);
       return false;
     }
@@ -90,9 +93,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
 
 // warp-wide bounded wait: lane 0 waits, the outcome is broadcast (use
 // before .sync.aligned tcgen05 instructions)
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, int *err) {
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, int *err,
+                                               long long budget = kWaitBudgetCycles) {
   uint32_t ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err);
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, budget);
   ok = __shfl_sync(0xffffffffu, ok, 0);
   __syncwarp();
   return ok != 0;
@@ -102,7 +106,8 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, i
 // per window, TMA threads with several stages of slack): between tries the
 // thread sleeps `ns` nanoseconds, so its polling does not take shared-memory
 // pipe slots from the warps that are doing the work
-__device__ __forceinline__ bool mbar_wait_lazy(uint64_t *bar, uint32_t parity, int *err, unsigned ns) {
+__device__ __forceinline__ bool mbar_wait_lazy(uint64_t *bar, uint32_t parity, int *err, unsigned ns,
+                                               long long budget = kWaitBudgetCycles) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
@@ -110,16 +115,17 @@ __device__ __forceinline__ bool mbar_wait_lazy(uint64_t *bar, uint32_t parity, i
     __nanosleep(ns);
     if (mbar_try_wait(a, parity)) return true;
     if (*(volatile int *)err) return false;
-    if (clock64() - t0 > kWaitBudgetCycles) {
+    if (clock64() - t0 > budget) {
       atomicExch(err, 1);
       return false;
     }
   }
 }
 
-__device__ __forceinline__ bool mbar_wait_lazy_warp(uint64_t *bar, uint32_t parity, int *err, unsigned ns) {
+__device__ __forceinline__ bool mbar_wait_lazy_warp(uint64_t *bar, uint32_t parity, int *err, unsigned ns,
+                                                    long long budget = kWaitBudgetCycles) {
   uint32_t ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait_lazy(bar, parity, err, ns);
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_lazy(bar, parity, err, ns, budget);
   ok = __shfl_sync(0xffffffffu, ok, 0);
   __syncwarp();
   return ok != 0;
@@ -127,11 +133,12 @@ __device__ __forceinline__ bool mbar_wait_lazy_warp(uint64_t *bar, uint32_t pari
 
 // bounded wait that ignores the error flag: used to drain copies / MMAs
 // still in flight before shared memory and TMEM are released
-__device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity,
+                                                long long budget = kWaitBudgetCycles) {
   const uint32_t a = smem_u32(bar);
   const long long t0 = clock64();
   while (!mbar_try_wait(a, parity))
-    if (clock64() - t0 > kWaitBudgetCycles) return false;
+    if (clock64() - t0 > budget) return false;
   return true;
 }
 
@@ -214,6 +221,18 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
       : "memory");
 }
 
+// A operand in tensor memory (lanes = rows of A, 16-bit elements packed two
+// per 32-bit column, element k of a row in column k / 2, low half first),
+// B from shared memory
+__device__ __forceinline__ void mma_f16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 // arrive on `bar` when every tcgen05.mma issued so far by this thread completes
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -250,6 +269,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 8 registers per thread -> 32 lanes x 8 consecutive 32-bit columns
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+               "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ bool elect_one() {
   uint32_t pred = 0;

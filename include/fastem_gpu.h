@@ -118,6 +118,19 @@ int fem_em_mstep(fem_em *h);
 /* EMAlgorithm::FindLargestConditionNumber (EM2/EMAlgorithm.cpp:193-202) */
 int fem_em_max_condition(fem_em *h, double *cond);
 
+/* Self-test of the bounded device waits (no counterpart in the reference,
+ * whose CPU loops have no device waits to bound; the reference's failure
+ * path it stands beside is the EMException of EM2/EMAlgorithm.cpp:147-163).
+ * Runs one small kernel with the roles of the mixed-precision kernels (a
+ * producer that never delivers, a consumer, a drain, two waiters off the
+ * critical path) whose waits give up after `budget_cycles` (1e3 .. 4e9):
+ * returns FEM_ERR_TIMEOUT with the message the real kernels' expiry produces,
+ * and *roles = bit mask of the waits that gave up (1 consumer, 2 drain, 4 and
+ * 8 the waiters that left on the status word).  The handle stays usable: the
+ * next call starts with the status word cleared.  Mixed-precision handles
+ * only (FEM_ERR_UNSUPPORTED otherwise). */
+int fem_em_selftest_wait_expiry(fem_em *h, int64_t budget_cycles, int *roles);
+
 /* EMAlgorithm::Posteriors (EM2/EMAlgorithm.h:41) after the last E-step, as
  * an n x k row-major double matrix. */
 int fem_em_get_posteriors(fem_em *h, double *post);
