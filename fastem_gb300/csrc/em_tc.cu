@@ -111,6 +111,38 @@ struct __align__(1024) CSmem {
 constexpr int kCThreads = (2 + kCProd + 4) * 32;   // warp 0 TMA, 1 MMA, 2..17 producers, 18..21 flush
 static_assert(sizeof(CSmem) + 1024 <= 232448, "covariance kernel shared memory");
 
+// covariance kernel, z x^T form: 4 components per CTA (2 pairs), 64-point blocks
+#ifndef FEM_COV_GROUPS
+#define FEM_COV_GROUPS 4
+#endif
+#ifndef FEM_COV_SPLIT
+#define FEM_COV_SPLIT 2
+#endif
+#ifndef FEM_COV_STAGGER
+#define FEM_COV_STAGGER 0
+#endif
+constexpr int kZIn = 6;                  // input ring (blocks)
+constexpr int kZA = 3;                   // TMEM A ring (blocks of 64 points, both pairs)
+constexpr int kZSets = FEM_COV_GROUPS;   // producer groups of 4 warps (one per TMEM lane quarter)
+constexpr int kZSplit = FEM_COV_SPLIT;   // groups sharing a block (each takes kBlk / 16 / kZSplit K steps)
+constexpr int kZStagger = FEM_COV_STAGGER;
+constexpr int kZN = 80;                  // accumulator columns per pair: 64 (x) + 16 (column 64 = sum z)
+constexpr uint32_t kZDCol = kZN;         // accumulator column pitch (pairs, buffers)
+constexpr uint32_t kZACol = 4 * kZN;     // first column of the A ring
+constexpr uint32_t kZAStage = 2 * (kBlk / 2);   // A columns per block: 2 pairs x 32 (64 FP16 points)
+constexpr int kZThreads = (2 + 4 * kZSets + 4) * 32;   // TMA, MMA, producers, flush
+constexpr int kZCols = kD + 1;           // flushed columns per pair row: 64 sums z x_b, then sum z
+struct __align__(1024) ZSmem {
+  __half bh[kZIn][kZN * kBlk];   // rows 0..63 X_h^T (TMA), row 64 ones, rows 65..79 zero (SW128)
+  __half bl[kZIn][kD * kBlk];    // X_l^T (TMA, SW128)
+  __half rh[kZIn][4 * kBlk];     // posteriors (hi part) of the CTA's 4 components
+  uint64_t in_full[kZIn], in_empty[kZIn], a_full[kZA], a_empty[kZA], acc_full[2], acc_empty[2], mma_done;
+  uint32_t tmem_base;
+};
+static_assert(sizeof(ZSmem) + 1024 <= 232448, "covariance kernel shared memory");
+static_assert(kZSets % kZSplit == 0 && (kBlk / 16) % kZSplit == 0, "covariance producer split");
+static_assert(kZACol + kZA * kZAStage <= 512 && 3 * kZDCol + kZN <= kZACol, "covariance kernel TMEM columns");
+
 struct TcEmPlan {
   CUtensorMap tm_xh, tm_xl, tm_wh, tm_wl;      // E-step
   CUtensorMap tm_rh, tm_rl, tm_xht, tm_xlt;    // means
@@ -784,6 +816,260 @@ __global__ void k_final_cov_tc(const double *__restrict__ cpart, const double *_
   }
 }
 
+// ====================================================== covariances (z x^T)
+// Sigma_j N_j = sum_i r_ij (x_i - mu_j)(x_i - mu_j)^T  (ComputeWeightedTempDataset
+// + BlockCovariances, EM2/MatrixEM.cpp:53-67,90-99), around the NEW means, as
+//   sum_i z_i x_i^T - (sum_i z_i) mu_j^T,   z_i = r_ij (x_i - mu_j),
+// with x = xh + xl (the FP16 split of X) on the B side, shared by every
+// component: the per-component operand z is formed once per (point,
+// component) by CUDA cores and written straight into tensor memory as the A
+// operand of an M = 128 (two components x 64 dimensions) MMA; B = [Xh^T; 1]
+// (N = 80, the ones row gives sum z in column 64) and Xl^T (N = 64) come from
+// global memory by TMA.  Every output element of an MMA is wanted (no
+// cross-component blocks), and the subtraction of (sum z) mu^T uses the sums
+// of the ROUNDED z, so FP16 rounding of z enters only as sum delta_i (x_i -
+// mu)^T: unbiased, centred, no diagonal correction needed.
+//
+// CTA (blockIdx.x = group of 4 components = 2 pairs, blockIdx.y = chunk of
+// 64-point blocks).  Warp 0: TMA; warp 1: MMA; warps 2..2+4 kZSets-1:
+// producers in groups of 4 (group = (warp - 2) / 4; kZSplit groups share a
+// block, each forming its own K steps, and the kZSets / kZSplit teams take
+// alternate blocks, so a block's operand is ready after a fraction of one
+// warp's work); a warp writes the TMEM lanes 32 (warp % 4) .. +31: dimension
+// 32 (warp & 1) + lane of the component in slot (warp & 3) / 2 of both pairs.
+// The last 4 warps flush the FP32 accumulators to FP64 partials every
+// kFlushBlocks blocks (double buffered in TMEM).
+__global__ void __launch_bounds__(kZThreads, 1)
+k_cov_zx(const __grid_constant__ CUtensorMap tm_xht, const __grid_constant__ CUtensorMap tm_xlt,
+         const __grid_constant__ CUtensorMap tm_rh4, const float *__restrict__ muf, int64_t n,
+         int64_t blocks_per_chunk, double *__restrict__ cpart, int *err) {
+  extern __shared__ uint8_t smem_raw[];
+  ZSmem &S = smem_aligned<ZSmem>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cg = blockIdx.x;
+  const int64_t nblocks = (n + kBlk - 1) / kBlk;
+  const int64_t b0 = (int64_t)blockIdx.y * blocks_per_chunk;
+  const int64_t mine = std::max<int64_t>(0, std::min<int64_t>(nblocks, b0 + blocks_per_chunk) - b0);
+  const int64_t nwin = (mine + kFlushBlocks - 1) / kFlushBlocks;
+  const size_t cta = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+
+  // constant rows 64..79 of the Bh stages (row 64 ones, the rest zero);
+  // 16-byte chunk c of row r stored at c ^ (r & 7)
+  for (int e = threadIdx.x; e < kZIn * 16 * kBlk; e += blockDim.x) {
+    const int st = e / (16 * kBlk), rem = e - st * 16 * kBlk;
+    const int r = 64 + rem / kBlk, col = rem % kBlk;
+    S.bh[st][r * kBlk + (((col >> 3) ^ (r & 7)) << 3) + (col & 7)] = __float2half(r == 64 ? 1.f : 0.f);
+  }
+  fence_proxy_async_smem();
+  if (threadIdx.x == 0) {
+    // a block is read by the MMA and by the kZSplit * 4 producer warps that form its operand
+    for (int st = 0; st < kZIn; st++) mbar_init(&S.in_full[st], 1), mbar_init(&S.in_empty[st], 4 * kZSplit + 1);
+    for (int st = 0; st < kZA; st++) mbar_init(&S.a_full[st], 4 * kZSplit), mbar_init(&S.a_empty[st], 1);
+    for (int b = 0; b < 2; b++) mbar_init(&S.acc_full[b], 1), mbar_init(&S.acc_empty[b], 4);
+    mbar_init(&S.mma_done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(&S.tmem_base, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem_base;
+  constexpr uint32_t kInBytes = 2 * kD * kBlk * 2 + 4 * kBlk * 2;
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA
+    if (elect_one()) {
+      bool ok = true;
+      for (int64_t t = 0; t < mine && ok; t++) {
+        const int st = (int)(t % kZIn);
+        if (!(ok = mbar_wait_lazy(&S.in_empty[st], ((t / kZIn) & 1) ^ 1, err, 128))) break;
+        // CTAs of the same point chunk (one per component group) start kZStagger
+        // blocks apart, so they do not all request the same tile at once
+        const int64_t tb = (t + (int64_t)cg * kZStagger) % mine;
+        const int p0 = (int)((b0 + tb) * kBlk);
+        mbar_expect_tx(&S.in_full[st], kInBytes);
+        tma_load_2d(S.bh[st], &tm_xht, &S.in_full[st], p0, 0);
+        tma_load_2d(S.bl[st], &tm_xlt, &S.in_full[st], p0, 0);
+        tma_load_2d(S.rh[st], &tm_rh4, &S.in_full[st], p0, cg * 4);
+      }
+      for (int64_t u = mine - 1; u >= 0 && u >= mine - kZIn; u--)
+        mbar_wait_drain(&S.in_full[u % kZIn], (u / kZIn) & 1);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA
+    if (elect_one()) {
+      bool ok = true;
+      constexpr uint32_t idh = idesc_f16(128, kZN), idl = idesc_f16(128, kD);
+      for (int64_t w = 0; w < nwin && ok; w++) {
+        const int ab = w & 1;
+        if (!(ok = mbar_wait(&S.acc_empty[ab], ((w >> 1) & 1) ^ 1, err))) break;
+        const int64_t t1 = std::min<int64_t>(mine, (w + 1) * kFlushBlocks);
+        for (int64_t t = w * kFlushBlocks; t < t1 && ok; t++) {
+          const int st = (int)(t % kZIn), sa = (int)(t % kZA);
+          if (!(ok = mbar_wait(&S.in_full[st], (t / kZIn) & 1, err))) break;
+          if (!(ok = mbar_wait(&S.a_full[sa], (t / kZA) & 1, err))) break;
+          tc_fence_after();
+          const uint64_t dbh = sdesc_sw128(smem_u32(S.bh[st])), dbl = sdesc_sw128(smem_u32(S.bl[st]));
+#pragma unroll
+          for (int kb = 0; kb < kBlk / 16; kb++) {
+#pragma unroll
+            for (int pr = 0; pr < 2; pr++) {
+              const uint32_t dt = tbase + ab * 2 * kZDCol + pr * kZDCol;
+              const uint32_t at = tbase + kZACol + sa * kZAStage + pr * (kBlk / 2) + kb * 8;
+              // +32 bytes per 16-point K step inside the 128-byte swizzle row
+              mma_f16_ta(dt, at, dbh + 2 * kb, idh, (t != w * kFlushBlocks) || kb);
+              mma_f16_ta(dt, at, dbl + 2 * kb, idl, 1);
+            }
+          }
+          mma_commit(&S.a_empty[sa]);
+          mma_commit(&S.in_empty[st]);
+        }
+        if (!ok) break;
+        mma_commit(&S.acc_full[ab]);
+      }
+      mma_commit(&S.mma_done);
+      mbar_wait_drain(&S.mma_done, 0);
+    }
+  } else if (warp < 2 + 4 * kZSets) {
+    // ------------------------------------------------ producers
+    const int pw = warp - 2, grp = pw >> 2, quad = warp & 3;
+    const int team = grp / kZSplit, part = grp % kZSplit;   // team: blocks; part: K steps within a block
+    constexpr int kTeams = kZSets / kZSplit, kSteps = kBlk / 16 / kZSplit;
+    const int slot = quad >> 1;                  // component slot within each pair
+    const int a = 32 * (quad & 1) + lane;        // dimension = TMEM lane within the slot
+    const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+    float mu[2];
+#pragma unroll
+    for (int pr = 0; pr < 2; pr++) mu[pr] = muf[(size_t)(cg * 4 + 2 * pr + slot) * kD + a];
+    bool ok = true;
+    for (int64_t t = team; t < mine && ok; t += kTeams) {
+      const int st = (int)(t % kZIn), sa = (int)(t % kZA);
+      if (!(ok = mbar_wait_warp(&S.in_full[st], (t / kZIn) & 1, err))) break;
+      if (!(ok = mbar_wait_warp(&S.a_empty[sa], ((t / kZA) & 1) ^ 1, err))) break;
+      tc_fence_after();
+      const uint8_t *rowh = reinterpret_cast<const uint8_t *>(S.bh[st]) + a * 128;
+      const uint8_t *rowl = reinterpret_cast<const uint8_t *>(S.bl[st]) + a * 128;
+#pragma unroll 1
+      for (int kb = part * kSteps; kb < (part + 1) * kSteps; kb++) {
+        // x = xh + xl (exact in FP32) of the 16 points of this K step, dimension a
+        float2 x[8];
+#pragma unroll
+        for (int hc = 0; hc < 2; hc++) {
+          const int c = 2 * kb + hc, pc = (c ^ (a & 7)) << 4;
+          const uint4 vh = *reinterpret_cast<const uint4 *>(rowh + pc);
+          const uint4 vl = *reinterpret_cast<const uint4 *>(rowl + pc);
+          const uint32_t wh[4] = {vh.x, vh.y, vh.z, vh.w}, wl[4] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+          for (int q = 0; q < 4; q++)
+            x[4 * hc + q] = __fadd2_rn(__half22float2(*reinterpret_cast<const __half2 *>(&wh[q])),
+                                       __half22float2(*reinterpret_cast<const __half2 *>(&wl[q])));
+        }
+#pragma unroll
+        for (int pr = 0; pr < 2; pr++) {
+          // z = fp16(x - mu) * r_hi, two points per half2 (the posteriors' hi
+          // part: an 11-bit weight, its rounding as random as z's own)
+          const uint4 *r4 = reinterpret_cast<const uint4 *>(S.rh[st] + (2 * pr + slot) * kBlk + 16 * kb);
+          const uint4 ra = r4[0], rb = r4[1];
+          const uint32_t rw[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+          const float2 nm = make_float2(-mu[pr], -mu[pr]);
+          uint32_t packed[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const float2 dz = __fadd2_rn(x[q], nm);
+            const __half2 z = __hmul2(__floats2half2_rn(dz.x, dz.y), *reinterpret_cast<const __half2 *>(&rw[q]));
+            packed[q] = *reinterpret_cast<const uint32_t *>(&z);
+          }
+          tmem_st8(tbase + lane_addr + kZACol + sa * kZAStage + pr * (kBlk / 2) + kb * 8, packed);
+        }
+      }
+      tmem_wait_st();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&S.a_full[sa]);
+        mbar_arrive(&S.in_empty[st]);
+      }
+    }
+  } else {
+    // ------------------------------------------------ flush warps
+    const int quad = warp & 3;
+    const int lrow = quad * 32 + lane;          // TMEM lane = row of the pair tile
+    // this CTA's FP64 partials, column-major per pair: column c of pair pr
+    // at o[pr][c * 128] (row lrow), so a warp's 32 rows are 256 contiguous bytes
+    double *o[2];
+#pragma unroll
+    for (int pr = 0; pr < 2; pr++) {
+      o[pr] = cpart + (cta * 2 + pr) * (size_t)(kZCols * 128) + lrow;
+      for (int c = 0; c < kZCols; c++) o[pr][(size_t)c * 128] = 0.0;
+    }
+    bool ok = true;
+    for (int64_t w = 0; w < nwin && ok; w++) {
+      const int ab = w & 1;
+      if (!(ok = mbar_wait_lazy_warp(&S.acc_full[ab], (w >> 1) & 1, err, 1000))) break;
+      tc_fence_after();
+#pragma unroll
+      for (int pr = 0; pr < 2; pr++) {
+        const uint32_t ta = tbase + ((uint32_t)(quad * 32) << 16) + ab * 2 * kZDCol + pr * kZDCol;
+#pragma unroll 1
+        for (int c0 = 0; c0 < kD; c0 += 16) {   // 16-column loads (the pair pitch is 80 columns)
+          uint32_t v[16];
+          tmem_ld16(ta + c0, v);
+          tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 16; c++) o[pr][(size_t)(c0 + c) * 128] += (double)__uint_as_float(v[c]);
+        }
+        uint32_t v16[16];
+        tmem_ld16(ta + kD, v16);
+        tmem_wait_ld();
+        o[pr][(size_t)kD * 128] += (double)__uint_as_float(v16[0]);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tbase, 512);
+}
+
+// Sigma_j = sym(sum z x^T - (sum z) muf^T) / N_j - (mu - muf)(mu - muf)^T:
+// the scatter around the FP32 means the producers used, moved to the FP64
+// means; chunks summed in order (FP64)
+__global__ void k_final_cov_zx(const double *__restrict__ cpart, int gx, int gy, int d,
+                               const double *__restrict__ psum, const double *__restrict__ mu,
+                               const float *__restrict__ muf, double *__restrict__ sigma) {
+  const int j = blockIdx.x, grp = j / 4, c = j % 4, pr = c >> 1, slot = c & 1;
+  __shared__ double sz[kD];                    // sum z of component j, per dimension
+  __shared__ double dm[kD];                    // mu - muf
+  for (int a = threadIdx.x; a < kD; a += blockDim.x) {
+    double v = 0.0;
+    for (int ch = 0; ch < gy; ch++)
+      v += cpart[(((size_t)ch * gx + grp) * 2 + pr) * (kZCols * 128) + (size_t)kD * 128 + slot * 64 + a];
+    sz[a] = v;
+    dm[a] = a < d ? mu[(size_t)j * d + a] - (double)muf[(size_t)j * kD + a] : 0.0;
+  }
+  __syncthreads();
+  const double inv = 1.0 / psum[j];
+  double *Sg = sigma + (size_t)j * d * d;
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    const int a = e / d, b = e - a * d;
+    if (b < a) continue;
+    double sab = 0.0, sba = 0.0;
+    for (int ch = 0; ch < gy; ch++) {
+      const double *P = cpart + (((size_t)ch * gx + grp) * 2 + pr) * (kZCols * 128) + slot * 64;
+      sab += P[(size_t)b * 128 + a];
+      sba += P[(size_t)a * 128 + b];
+    }
+    const double ca = sab - sz[a] * (double)muf[(size_t)j * kD + b];
+    const double cb = sba - sz[b] * (double)muf[(size_t)j * kD + a];
+    const double v = 0.5 * (ca + cb) * inv - dm[a] * dm[b];
+    Sg[a * d + b] = v;
+    Sg[b * d + a] = v;
+  }
+}
+
 // ================================================= bounded-wait expiry
 // The exit path every warp-specialised kernel here relies on, run on purpose:
 // one CTA with the roles of those kernels, whose producer never delivers.
@@ -947,6 +1233,7 @@ __global__ void k_classes_tc(const __half *__restrict__ Rh, const __half *__rest
 static size_t esmem_bytes() { return sizeof(ESmem) + 1024; }
 static size_t msmem_bytes() { return sizeof(MSmem) + 1024; }
 static size_t csmem_bytes() { return sizeof(CSmem) + 1024; }
+static size_t zsmem_bytes() { return sizeof(ZSmem) + 1024; }
 
 static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t rows, uint64_t pitch_elems,
                     uint32_t box_cols, uint32_t box_rows, CUtensorMapSwizzle swz) {
@@ -963,6 +1250,16 @@ bool em_tc_supported(int d, int k) { return d >= 1 && d <= kD && k >= 1 && k <= 
 // than 16384 points per component on average it would not, so such fits take
 // the FP32 CUDA-core covariance (its cost is small at that size).
 bool em_tc_small_components(int64_t n, int k) { return n < (int64_t)16384 * k; }
+
+// covariance kernel selection while both forms are compared (FEM_COV_KERNEL=zz
+// selects the z z^T form)
+static bool cov_zx_enabled() {
+  static const bool zx = [] {
+    const char *v = getenv("FEM_COV_KERNEL");
+    return !(v && v[0] == 'z' && v[1] == 'z');
+  }();
+  return zx;
+}
 
 int em_tc_create(fem_em *h) {
   TcEmPlan *p = new TcEmPlan();
@@ -1000,7 +1297,7 @@ int em_tc_create(fem_em *h) {
   FEM_TRY(dalloc(&p->mpart, (size_t)p->mgrid * kMaxK * kMeanN));
   p->cgx = K / 4;
   p->cgy = (int)std::max<int64_t>(1, std::min<int64_t>(nblocks, (4 * sms + p->cgx - 1) / p->cgx));
-  FEM_TRY(dalloc(&p->cpart, (size_t)p->cgx * p->cgy * 4 * kD * kD));
+  FEM_TRY(dalloc(&p->cpart, (size_t)p->cgx * p->cgy * std::max(4 * kD * kD, 2 * kZCols * 128)));
   FEM_TRY(dalloc(&p->dpart, (size_t)p->cgx * p->cgy * 4 * kD));
   // E-step operands
   FEM_TRY(fp16_map(&p->tm_xh, h->Xhi, kD, n, kD, kD, kTileM, CU_TENSOR_MAP_SWIZZLE_128B));
@@ -1027,6 +1324,7 @@ int em_tc_create(fem_em *h) {
   FEM_CUDA(cudaFuncSetAttribute(k_estep_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem_bytes()));
   FEM_CUDA(cudaFuncSetAttribute(k_means_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)msmem_bytes()));
   FEM_CUDA(cudaFuncSetAttribute(k_cov_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem_bytes()));
+  FEM_CUDA(cudaFuncSetAttribute(k_cov_zx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsmem_bytes()));
   return FEM_OK;
 }
 
@@ -1116,11 +1414,19 @@ int em_tc_mstep(fem_em *h) {
   const int64_t nblocks = (h->n + kBlk - 1) / kBlk;
   const int64_t bpc = (nblocks + p->cgy - 1) / p->cgy;
   timing_begin(h, 8);
-  k_cov_tc<<<dim3(p->cgx, p->cgy), kCThreads, csmem_bytes(), h->stream>>>(p->tm_x32, p->tm_rh4, p->tm_rl4, p->muf,
-                                                                         h->n, bpc, p->cpart, p->dpart, p->err);
-  FEM_CUDA(cudaGetLastError());
-  timing_begin(h, 9);
-  k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->d, h->psum, h->sigma);
+  if (cov_zx_enabled()) {
+    k_cov_zx<<<dim3(p->cgx, p->cgy), kZThreads, zsmem_bytes(), h->stream>>>(p->tm_xht, p->tm_xlt, p->tm_rh4, p->muf,
+                                                                           h->n, bpc, p->cpart, p->err);
+    FEM_CUDA(cudaGetLastError());
+    timing_begin(h, 9);
+    k_final_cov_zx<<<K, 256, 0, h->stream>>>(p->cpart, p->cgx, p->cgy, h->d, h->psum, h->mu, p->muf, h->sigma);
+  } else {
+    k_cov_tc<<<dim3(p->cgx, p->cgy), kCThreads, csmem_bytes(), h->stream>>>(p->tm_x32, p->tm_rh4, p->tm_rl4, p->muf,
+                                                                           h->n, bpc, p->cpart, p->dpart, p->err);
+    FEM_CUDA(cudaGetLastError());
+    timing_begin(h, 9);
+    k_final_cov_tc<<<K, 256, 0, h->stream>>>(p->cpart, p->dpart, p->cgx, p->cgy, h->d, h->psum, h->sigma);
+  }
   FEM_CUDA(cudaGetLastError());
   k_flag_timeout<<<1, 32, 0, h->stream>>>(h->dstat, p->err);
   h->launches += 5;
