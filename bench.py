@@ -872,10 +872,27 @@ KM_PROFILE_FILE = os.path.join(ROOT, "profiles", "kmeans_assign_n16m_d32_k256.md
 
 
 def km_workload(n, d, k):
-    from fastem_gb300 import synth
+    """Equal isotropic blobs (sigma 1, centres U[-20, 20]^d), k-means||
+    seeding with seed 3 (KMeansOrOrInitializer, Clust/KMeansOrOrInitializer.cpp:
+    143-174) by the library's own host seeder (`em2gpu --seed oror`, the
+    reference's draw order on one generator stream; its rows equal the
+    oracle's restatement in tests/test_host.py).  Returns (X, C0, seconds the
+    seeding took)."""
+    import tempfile
+    from fastem_gb300 import build as B
+    from fastem_gb300 import formats, synth
     X, _ = synth.kmeans_blobs(seed=2, n=n, d=d, k=k)
-    C0 = synth.dsquared_init(X, k, seed=3)[1].copy()
-    return X, C0
+    B.build_host()
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "x.bin")
+        formats.write_bin(f, X)
+        t0 = time.perf_counter()
+        out = subprocess.run([B.EM2GPU, "--seed", "oror", f, str(k), "3"], capture_output=True, text=True,
+                             check=True)
+        secs = time.perf_counter() - t0
+    C0 = np.array([[float(v) for v in ln.split()] for ln in out.stdout.strip().splitlines()])
+    assert C0.shape == (k, d)
+    return X, np.ascontiguousarray(C0), secs
 
 
 def time_km_iterations(km, C, warmup, steps, dist):
@@ -898,15 +915,19 @@ def time_km_iterations(km, C, warmup, steps, dist):
 
 def run_kmeans(args, rank, world, local):
     """Lloyd k-means at N = 2^24, d = 32, K = 256 (equal isotropic blobs,
-    sigma 1, centres U[-20, 20]^32; D^2-sampled initial centroids): mixed
+    sigma 1, centres U[-20, 20]^32; k-means|| seeding, seed 3): mixed
     (tcgen05 GEMM + argmin, FP32 refinement, FP64 recheck) against the FP32
-    CUDA-core path; roofline = HBM (read X once, write labels)."""
+    CUDA-core path; roofline = HBM (read X once, write labels).  Outside the
+    timed region both paths run the configuration's 30 iterations from the
+    same centroids and their labels are compared after every iteration; the
+    CPU leg checks the first iteration's labels of its row sample against the
+    oracle's FP64 assignment."""
     import torch
     from fastem_gb300 import CudaKMA
     n, d, k = args.n, 32, 256
     if args.impl == "reference":
         if rank == 0:
-            X, C0 = km_workload(n, d, k)
+            X, C0, _ = km_workload(n, d, k)
             cpu = km_cpu_baseline(X, C0)
             print(json.dumps({"metric": KM_METRIC, "impl": "reference", "value": cpu["value"], "unit": UNIT,
                               "n_gpus": world, "steps": 1, "warmup": 1, "higher_is_better": True,
@@ -916,7 +937,7 @@ def run_kmeans(args, rank, world, local):
         return
     dist = Dist(world)
     torch.cuda.set_device(local)
-    X, C0 = km_workload(n, d, k)
+    X, C0, seed_s = km_workload(n, d, k)
     algo_bytes = n * d * 4 + n * 4
     with CudaKMA(d, n, k, precision="mixed", device=local, repair=True) as km:
         km.SetDataset(X)
@@ -953,7 +974,29 @@ def run_kmeans(args, rank, world, local):
             a32, u32, _, r32 = time_km_iterations(k32, C32, 1, max(2, args.steps // 3), dist)
             ms32 = dist.max(a32 + u32) / max(2, args.steps // 3)
             fp32 = {"value": world * 1e3 / ms32, "ms_per_step": ms32, "rechecked_rows": r32}
-    cpu = km_cpu_baseline(X, C0) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    # the configuration's 30 iterations through both GPU paths, labels compared each time
+    parity, first_labels = None, None
+    if not args.no_fp32:
+        iters, mism, dmax, fmax = 30, 0, 0.0, 0.0
+        Cm, Cf = C0.copy(), C0.copy()
+        with CudaKMA(d, n, k, precision="mixed", device=local, repair=True) as km1, \
+                CudaKMA(d, n, k, precision="fp32", device=local, repair=True) as km2:
+            km1.SetDataset(X)
+            km2.SetDataset(X)
+            km1.InitDataStructures()
+            km2.InitDataStructures()
+            for it in range(iters):
+                f1 = km1.ComputeMSEAndCorrect(Cm)
+                f2 = km2.ComputeMSEAndCorrect(Cf)
+                l1, l2 = km1.Assignment(), km2.Assignment()
+                if it == 0:
+                    first_labels = l1.copy()
+                mism += int((l1 != l2).sum())
+                dmax = max(dmax, float(np.max(np.abs(Cm - Cf))))
+                fmax = max(fmax, abs(f1 - f2) / abs(f2))
+        parity = {"iterations": iters, "label_mismatches_mixed_vs_fp32": mism,
+                  "max_centroid_difference": dmax, "max_fit_rel_difference": fmax}
+    cpu = km_cpu_baseline(X, C0, first_labels) if (rank == 0 and world == 1 and not args.no_cpu) else None
     dist.close()
     if rank != 0:
         return
@@ -978,21 +1021,23 @@ def run_kmeans(args, rank, world, local):
         "vs_baseline": None, "dtype": "fp16x3 distances, fp32 refinement, fp64 recheck",
         "data": "synthetic kmeans_blobs (seeded; equal isotropic blobs, sigma 1, centres U[-20,20]^32)",
         "config": {"workload": "kmeans_blobs N=%d d=%d K=%d, one Lloyd iteration per step" % (n, d, k),
-                   "n": n, "d": d, "k": k, "init": "D^2 sampling on a 65536-row sample (seed 3)",
+                   "n": n, "d": d, "k": k, "init": "k-means|| (seed 3, %.1f s on the host)" % seed_s,
                    "l2": "inputs larger than L2 (X 2.1 GB)"},
         "roofline": {"kernel": "k_km_assign_tc", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": assign_ms},
-        "rechecked_rows_last_step": rech, "e2e": e2e, "fp32_plain": fp32,
+        "rechecked_rows_last_step": rech, "parity": parity, "e2e": e2e, "fp32_plain": fp32,
         "speedup_vs_fp32_plain": (value / fp32["value"]) if fp32 else None,
         "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
 
 
-def km_cpu_baseline(X, C0):
+def km_cpu_baseline(X, C0, gpu_labels=None):
     """The oracle's Lloyd iteration (FP64, OpenMP, all host cores) on the
-    first 2^20 rows, scaled to N."""
+    first 2^20 rows, scaled to N.  With `gpu_labels` (the GPU's first-iteration
+    assignment of all rows from the same centroids) the sample's labels are
+    compared: an assignment depends only on the row and the centroids."""
     from oracle import oracle as O
     O.lib()
     n = len(X)
@@ -1001,10 +1046,13 @@ def km_cpu_baseline(X, C0):
     Xs = np.ascontiguousarray(X[:sample])
     O.km_iterate(Xs[:4096], C0.copy(), repair=False, nthreads=threads)
     t0 = time.perf_counter()
-    O.km_iterate(Xs, C0.copy(), repair=False, nthreads=threads)
+    _, _, _, labels = O.km_iterate(Xs, C0.copy(), repair=False, nthreads=threads)
     dt = (time.perf_counter() - t0) * n / sample
-    return {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "1 FP64 iteration over the first %d of %d rows, scaled x%d" % (sample, n, n // sample)}
+    out = {"value": 1.0 / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": "1 FP64 iteration over the first %d of %d rows, scaled x%d" % (sample, n, n // sample)}
+    if gpu_labels is not None:
+        out["label_mismatches_vs_gpu_first_iteration"] = int((labels != gpu_labels[:sample]).sum())
+    return out
 
 
 if __name__ == "__main__":
