@@ -67,7 +67,7 @@ int reset_status(fem_em *h) {
   s.chol_failed = INT_MAX;
   *h->hstat = s;
   FEM_CUDA(cudaMemcpyAsync(h->dstat, h->hstat, sizeof(DevStatus), cudaMemcpyHostToDevice, h->stream));
-  if (mixed(h) && h->tc) FEM_TRY(em_tc_reset_err(h));
+  if (mixed(h) && (h->tc || h->wide)) FEM_TRY(em_tc_reset_err(h));
   return FEM_OK;
 }
 
@@ -114,7 +114,7 @@ int cond_check(fem_em *h, double *cond) {
 }
 
 void free_all(fem_em *h) {
-  if (h->tc) em_tc_destroy(h);
+  if (h->tc || h->wide) em_tc_destroy(h);
   dfree(h->X);
   dfree(h->Xhi);
   dfree(h->Xlo);
@@ -178,8 +178,8 @@ int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **ou
     return FEM_ERR_BAD_ARG;
   }
   if (c.precision == FEM_PREC_MIXED && !em_tc_supported(d, k)) {
-    set_error("mixed precision (tensor-core kernels) needs d <= 64 and k <= 128 (got d=%d k=%d); "
-              "use FEM_PREC_FP32 or FEM_PREC_FP64", d, k);
+    set_error("mixed precision (tensor-core kernels) needs d <= 64 and k <= 128, or 64 < d <= 256 "
+              "(got d=%d k=%d); use FEM_PREC_FP32 or FEM_PREC_FP64", d, k);
     return FEM_ERR_UNSUPPORTED;
   }
   FEM_TRY(select_device(c.device));
@@ -226,7 +226,7 @@ int fem_em_create(int d, int64_t n, int k, const fem_em_config *cfg, fem_em **ou
   if (c.precision == FEM_PREC_MIXED) {
     st = em_tc_create(h);
     if (st) return fail(st);
-    if (em_tc_small_components(n, k)) {
+    if (em_tc_small_components(n, k, d)) {
       // partials of the FP32 CUDA-core covariance used for small components
       int TB, nb, nblk;
       cov_geometry(d, &TB, &nb, &nblk);
@@ -374,7 +374,7 @@ int fem_em_mstep(fem_em *h) {
 int fem_em_selftest_wait_expiry(fem_em *h, int64_t budget_cycles, int *roles) {
   FEM_TRY(check_handle(h));
   if (!mixed(h) || !h->tc) {
-    set_error("the bounded-wait self-test runs on a mixed-precision handle");
+    set_error("the bounded-wait self-test runs on a mixed-precision handle with d <= 64");
     return FEM_ERR_UNSUPPORTED;
   }
   if (!roles || budget_cycles < 1000 || budget_cycles > 4000000000LL) {

@@ -26,7 +26,7 @@ int em_tc_mstep(fem_em *h);
 // posteriors as FP16 hi + lo, means as float with row stride mu_ld
 int em_cov_hilo(fem_em *h, const __half *Rh, const __half *Rl, int64_t pitch, const float *muf, int mu_ld);
 // true when the mixed path computes covariances with em_cov_hilo
-bool em_tc_small_components(int64_t n, int k);
+bool em_tc_small_components(int64_t n, int k, int d);
 // device posteriors of the mixed path: FP16 hi / lo, component-major, row pitch
 void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch);
 // records event `slot` on the handle's stream when timing is enabled
@@ -38,6 +38,20 @@ int em_tc_reset_err(fem_em *h);
 // runs the bounded-wait expiry self-test kernel; *roles = bit mask of the
 // waits that gave up (1 consumer, 2 drain, 4 and 8 the two flag-driven waiters)
 int em_tc_wait_selftest(fem_em *h, long long budget, int *roles);
+
+// em_wide.cu (tcgen05 split precision, 64 < d <= 256; em_tc_* dispatch here
+// when the handle's d is above 64)
+bool em_wide_supported(int d, int k);
+int em_wide_create(fem_em *h);
+void em_wide_destroy(fem_em *h);
+int em_wide_upload(fem_em *h);
+int em_wide_prepare(fem_em *h);
+int em_wide_estep(fem_em *h);
+int em_wide_mstep(fem_em *h);
+int em_wide_reset_err(fem_em *h);
+int em_wide_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout);
+void em_wide_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch);
+int em_wide_classes(fem_em *h, int32_t *dcls);
 
 // host_linalg.cpp
 // largest condition number of the K covariances (FP64 Jacobi on the device)

@@ -1243,13 +1243,15 @@ static int fp16_map(CUtensorMap *m, const void *base, uint64_t cols, uint64_t ro
 
 // the covariance kernel works on groups of 4 components
 // d <= 64 (zero-padded to 64) and K <= 128 (padded to a multiple of 4)
-bool em_tc_supported(int d, int k) { return d >= 1 && d <= kD && k >= 1 && k <= kMaxK; }
+bool em_tc_supported(int d, int k) {
+  return (d >= 1 && d <= kD && k >= 1 && k <= kMaxK) || em_wide_supported(d, k);
+}
 
 // The tensor-core covariance rounds z to FP16 once; that error averages out
 // over the points of a component (relative ~2^-12 / sqrt(N_j)).  With fewer
 // than 16384 points per component on average it would not, so such fits take
 // the FP32 CUDA-core covariance (its cost is small at that size).
-bool em_tc_small_components(int64_t n, int k) { return n < (int64_t)16384 * k; }
+bool em_tc_small_components(int64_t n, int k, int d) { return d <= kD && n < (int64_t)16384 * k; }
 
 // covariance kernel selection while both forms are compared (FEM_COV_KERNEL=zz
 // selects the z z^T form)
@@ -1262,6 +1264,7 @@ static bool cov_zx_enabled() {
 }
 
 int em_tc_create(fem_em *h) {
+  if (h->d > kD) return em_wide_create(h);
   TcEmPlan *p = new TcEmPlan();
   h->tc = p;
   const int K = (h->k + 3) / 4 * 4;     // kernels see K padded to a multiple of 4
@@ -1329,6 +1332,7 @@ int em_tc_create(fem_em *h) {
 }
 
 void em_tc_destroy(fem_em *h) {
+  em_wide_destroy(h);
   TcEmPlan *p = h->tc;
   if (!p) return;
   dfree(p->Wh);
@@ -1355,6 +1359,7 @@ void em_tc_destroy(fem_em *h) {
 }
 
 int em_tc_upload(fem_em *h) {
+  if (h->wide) return em_wide_upload(h);
   TcEmPlan *p = h->tc;
   float *amax = p->amax;
   FEM_CUDA(cudaMemsetAsync(amax, 0, sizeof(float), h->stream));
@@ -1375,6 +1380,7 @@ int em_tc_upload(fem_em *h) {
 }
 
 int em_tc_prepare(fem_em *h) {
+  if (h->wide) return em_wide_prepare(h);
   TcEmPlan *p = h->tc;
   k_prep_w<<<p->kp, 256, 0, h->stream>>>(h->linv, h->mu, h->k, h->d, p->Wh, p->Wl, p->bias, h->logc, p->chi,
                                          p->clo);
@@ -1384,6 +1390,7 @@ int em_tc_prepare(fem_em *h) {
 }
 
 int em_tc_estep(fem_em *h) {
+  if (h->wide) return em_wide_estep(h);
   TcEmPlan *p = h->tc;
   k_estep_tc<<<p->egrid, kEThreads, esmem_bytes(), h->stream>>>(
       p->tm_xh, p->tm_xl, p->tm_wh, p->tm_wl, p->bias, p->chi, p->clo, h->logc, p->lsc, p->Rh, p->Rl, p->np,
@@ -1396,6 +1403,7 @@ int em_tc_estep(fem_em *h) {
 }
 
 int em_tc_mstep(fem_em *h) {
+  if (h->wide) return em_wide_mstep(h);
   TcEmPlan *p = h->tc;
   const int K = h->k;
   k_means_tc<<<p->mgrid, 192, msmem_bytes(), h->stream>>>(p->tm_rh, p->tm_rl, p->tm_xht, p->tm_xlt, h->n,
@@ -1403,7 +1411,7 @@ int em_tc_mstep(fem_em *h) {
   FEM_CUDA(cudaGetLastError());
   k_final_means_tc<<<K, 64, 0, h->stream>>>(p->mpart, p->mgrid, K, h->d, h->n, h->mu, h->pi, h->psum, p->muf);
   FEM_CUDA(cudaGetLastError());
-  if (em_tc_small_components(h->n, h->k)) {
+  if (em_tc_small_components(h->n, h->k, h->d)) {
     timing_begin(h, 8);
     FEM_TRY(em_cov_hilo(h, p->Rh, p->Rl, p->np, p->muf, kD));
     timing_begin(h, 9);
@@ -1436,6 +1444,7 @@ int em_tc_mstep(fem_em *h) {
 // a wait that ran out in an earlier call leaves the status word set; each new
 // call starts from zero (the context itself stays usable: nothing faulted)
 int em_tc_reset_err(fem_em *h) {
+  if (h->wide) return em_wide_reset_err(h);
   FEM_CUDA(cudaMemsetAsync(h->tc->err, 0, sizeof(int), h->stream));
   return FEM_OK;
 }
@@ -1456,6 +1465,7 @@ int em_tc_wait_selftest(fem_em *h, long long budget, int *roles) {
 }
 
 int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout) {
+  if (h->wide) return em_wide_post_rows(h, r0, rows, dout);
   TcEmPlan *p = h->tc;
   const int64_t tot = rows * h->k;
   k_post_rows_tc<<<(unsigned)((tot + 255) / 256), 256, 0, h->stream>>>(p->Rh, p->Rl, p->np, h->k, r0, rows, dout);
@@ -1464,12 +1474,14 @@ int em_tc_post_rows(fem_em *h, int64_t r0, int64_t rows, double *dout) {
 }
 
 void em_tc_posteriors(fem_em *h, const __half **rh, const __half **rl, int64_t *pitch) {
+  if (h->wide) return em_wide_posteriors(h, rh, rl, pitch);
   *rh = h->tc->Rh;
   *rl = h->tc->Rl;
   *pitch = h->tc->np;
 }
 
 int em_tc_classes(fem_em *h, int32_t *dcls) {
+  if (h->wide) return em_wide_classes(h, dcls);
   TcEmPlan *p = h->tc;
   k_classes_tc<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(p->Rh, p->Rl, p->np, h->n, h->k, dcls);
   FEM_CUDA(cudaGetLastError());

@@ -91,7 +91,8 @@ struct DevStatus {
 enum { EM_PAR_CHUNKS = 0 };
 
 struct EmHandle;
-struct TcEmPlan;  // mixed-precision launch plan (em_tc.cu)
+struct TcEmPlan;    // mixed-precision launch plan, d <= 64 (em_tc.cu)
+struct WideEmPlan;  // mixed-precision launch plan, 64 < d <= 256 (em_wide.cu)
 
 }  // namespace fem
 
@@ -131,6 +132,7 @@ struct fem_em {
 
   // mixed-precision state (em_tc.cu)
   fem::TcEmPlan *tc = nullptr;
+  fem::WideEmPlan *wide = nullptr;
 
   fem::DevStatus *dstat = nullptr;   // device
   fem::DevStatus *hstat = nullptr;   // pinned host

@@ -234,8 +234,6 @@ def test_illcond_d256_fp64_matches_oracle(gpu_lib, oracle):
     np.testing.assert_allclose(ll, ref["logl"], rtol=1e-10)
     np.testing.assert_allclose(G.means, ref["mu"], rtol=1e-7, atol=1e-8)
     assert 1e5 < cond < 1e7
-    with pytest.raises(Exception, match="mixed precision"):
-        CudaMatrixEM(d, n, k, precision="mixed")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32", "mixed"])

@@ -172,13 +172,20 @@ def test_em2gpu_kmeans_init_mixed_and_unsupported_width(em2gpu, tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     final = float(out.stdout.split("Final loglikelihood:")[1].split()[0])
     assert np.isfinite(final)
-    # mixed precision runs d <= 64 (zero-padded); d = 80 is refused with a message
+    # mixed precision runs d <= 64 (zero-padded) and 64 < d <= 256 (the wide kernels)
     ok = subprocess.run([em2gpu, fb, "-c", "6", "-p", "mixed", "-m", "3", "-I", "kmeans"], capture_output=True,
                         text=True, timeout=300)
     assert ok.returncode == 0, ok.stdout + ok.stderr
     fw = str(tmp_path / "wide.bin")
     formats.write_bin(fw, np.random.default_rng(1).standard_normal((5000, 80)).astype(np.float32))
-    bad = subprocess.run([em2gpu, fw, "-c", "4", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
+    wide = subprocess.run([em2gpu, fw, "-c", "4", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
+                          timeout=300)
+    assert wide.returncode == 0, wide.stdout + wide.stderr
+    assert np.isfinite(float(wide.stdout.split("Final loglikelihood:")[1].split()[0]))
+    # values outside the FP16 operand range are refused with a message
+    fh = str(tmp_path / "huge.bin")
+    formats.write_bin(fh, (np.random.default_rng(2).standard_normal((5000, 80)) * 1e5).astype(np.float32))
+    bad = subprocess.run([em2gpu, fh, "-c", "4", "-p", "mixed", "-m", "2"], capture_output=True, text=True,
                          timeout=300)
     assert bad.returncode == 1 and "mixed precision" in bad.stderr
     # the k-means|| EM initializer (KMeansOrOrEMInitializer)
