@@ -40,8 +40,12 @@
 //  3. k_wide_cov: z = fp16(sqrt r) * y for 64-point blocks of one component,
 //     M = z z^T (two M = 128 products: dims 0..127 x 0..127 and 128..255 x
 //     0..255) in FP32 TMEM windows of 4096 points, flushed to FP64; producers
-//     also sum r and r y.  The (component, block) space is split evenly over
-//     the CTAs.
+//     also sum r, r y and the diagonal z_a^2 in FP32 (round to nearest).  The
+//     tensor core's FP32 accumulation drops an addend's bits below the
+//     accumulator's ulp (toward zero): harmless for the off-diagonal sums,
+//     whose increments have either sign, but the diagonal's increments are
+//     all positive and would be biased low.  The (component, block) space is
+//     split evenly over the CTAs.
 //  4. k_wide_gather + k_wide_gemm: FP64 finalisation per component (means,
 //     weights, M - ybar ybar^T, L M L^T).
 //
@@ -69,12 +73,17 @@ constexpr int kWTile = 128;         // E-step points per tile (MMA M)
 constexpr int kWAS = 2;             // centred-x operand ring (64-dim chunks)
 constexpr int kWWS = 2;             // W operand ring (64-dim chunks)
 constexpr uint32_t kWXCol = 256;    // TMEM column of the tile's FP32 rows
-constexpr int kWEThreads = 320;     // warp 0 TMA, 1 MMA, 2..5 producers, 6..9 epilogue
+// warp 0 TMA, 1 MMA, 2..5 producers, 6..13 epilogue (two groups of 4 warps that
+// read alternate 64-column quarters).  14 warps are allocated as 16, which
+// leaves 128 registers per thread.
+constexpr int kWEThreads = 448;
+constexpr int kWEpi0 = 6;           // first epilogue warp
 constexpr int kVBlk = 64;           // covariance kernel: points per block
 constexpr int kVS = 5;              // covariance input ring
 constexpr int kVWin = 64;           // blocks per FP32 accumulation window (4096 points)
 constexpr int kWCThreads = 320;     // warp 0 TMA, 1 MMA, 2..5 producers, 6..9 flush
-constexpr int kSPart = kWMax + kVBlk;   // per (CTA, component) sums: r y (kWMax), r (64 partials)
+// per (CTA, component) sums: r y (kWMax), z_a^2 (kWMax), r (64 partials)
+constexpr int kSPart = 2 * kWMax + kVBlk;
 constexpr int kWMaxGrid = 256;      // covariance CTAs at most (a component may meet all of them)
 
 struct __align__(1024) WESmem {
@@ -85,6 +94,7 @@ struct __align__(1024) WESmem {
   uint64_t a_full[kWAS], a_empty[kWAS], w_full[kWWS], w_empty[kWWS];
   uint64_t acc_full, acc_empty[4], mma_done;
   uint32_t tmem_base;
+  float ssum[2][kWTile];          // second epilogue group's partial sums of y^2 (by unit parity)
   double red[4];
 };
 static_assert(sizeof(WESmem) + 1024 <= 232448, "wide E-step shared memory");
@@ -277,7 +287,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       mma_commit(&S.mma_done);
       mbar_wait_drain(&S.mma_done, 0);
     }
-  } else if (warp < 6) {
+  } else if (warp < kWEpi0) {
     // ------------------------------------------------ producers: a = x - m -> FP16 hi / lo
     const int quad = warp & 3, row = quad * 32 + lane;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
@@ -287,12 +297,12 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       const int64_t pt = tile * kWTile + row;
       const bool live = pt < n;
       const float *xr = X + (live ? pt : 0) * (int64_t)d;
-      // this tile's FP32 row -> TMEM columns kWXCol ..
+      // this group's part of the tile's FP32 row -> TMEM columns kWXCol ..
       for (int c = 0; c < nc; c++) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int pg = 0; pg < 2; pg++) {
           uint32_t v[32];
-          const int c0 = 64 * c + 32 * h;
+          const int c0 = 64 * c + 32 * pg;
           if ((d & 3) == 0) {
 #pragma unroll
             for (int e = 0; e < 32; e += 4) {
@@ -314,30 +324,35 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
         for (int c = nc - 1; c >= 0; c--) {
           const int sa = ai % kWAS;
           if (!(ok = mbar_wait_warp(&S.a_empty[sa], ((ai / kWAS) & 1) ^ 1, err))) break;
-          uint32_t x[64];
-          tmem_ld64(tbase + lane_addr + kWXCol + 64 * c, x);
-          tmem_wait_ld();
           uint8_t *dh = reinterpret_cast<uint8_t *>(S.ah[sa]) + row * 128;
           uint8_t *dl = reinterpret_cast<uint8_t *>(S.al[sa]) + row * 128;
 #pragma unroll
-          for (int q = 0; q < 8; q++) {
-            const float4 m0 = __ldg(reinterpret_cast<const float4 *>(mj + 64 * c + 8 * q));
-            const float4 m1 = __ldg(reinterpret_cast<const float4 *>(mj + 64 * c + 8 * q + 4));
-            const float a[8] = {__uint_as_float(x[8 * q]) - m0.x,     __uint_as_float(x[8 * q + 1]) - m0.y,
-                                __uint_as_float(x[8 * q + 2]) - m0.z, __uint_as_float(x[8 * q + 3]) - m0.w,
-                                __uint_as_float(x[8 * q + 4]) - m1.x, __uint_as_float(x[8 * q + 5]) - m1.y,
-                                __uint_as_float(x[8 * q + 6]) - m1.z, __uint_as_float(x[8 * q + 7]) - m1.w};
-            uint32_t hw[4], lw[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-              const __half2 hh = __floats2half2_rn(a[2 * u], a[2 * u + 1]);
-              const float2 f = __half22float2(hh);
-              hw[u] = h2_bits(hh);
-              lw[u] = h2_bits(__floats2half2_rn(a[2 * u] - f.x, a[2 * u + 1] - f.y));
+          for (int pg = 0; pg < 2; pg++) {   // two 32-dim halves of the chunk
+            uint32_t x[32];
+            tmem_ld32(tbase + lane_addr + kWXCol + 64 * c + 32 * pg, x);
+            tmem_wait_ld();
+            const float *mc = mj + 64 * c + 32 * pg;
+  #pragma unroll
+            for (int qq = 0; qq < 4; qq++) {
+              const int q = 4 * pg + qq;    // 16-byte chunk of the 128-byte operand row
+              const float4 m0 = __ldg(reinterpret_cast<const float4 *>(mc + 8 * qq));
+              const float4 m1 = __ldg(reinterpret_cast<const float4 *>(mc + 8 * qq + 4));
+              const float a[8] = {__uint_as_float(x[8 * qq]) - m0.x,     __uint_as_float(x[8 * qq + 1]) - m0.y,
+                                  __uint_as_float(x[8 * qq + 2]) - m0.z, __uint_as_float(x[8 * qq + 3]) - m0.w,
+                                  __uint_as_float(x[8 * qq + 4]) - m1.x, __uint_as_float(x[8 * qq + 5]) - m1.y,
+                                  __uint_as_float(x[8 * qq + 6]) - m1.z, __uint_as_float(x[8 * qq + 7]) - m1.w};
+              uint32_t hw[4], lw[4];
+  #pragma unroll
+              for (int u = 0; u < 4; u++) {
+                const __half2 hh = __floats2half2_rn(a[2 * u], a[2 * u + 1]);
+                const float2 f = __half22float2(hh);
+                hw[u] = h2_bits(hh);
+                lw[u] = h2_bits(__floats2half2_rn(a[2 * u] - f.x, a[2 * u + 1] - f.y));
+              }
+              const int off = (q ^ (row & 7)) << 4;   // 128-byte swizzle of 16-byte chunks
+              *reinterpret_cast<uint4 *>(dh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+              *reinterpret_cast<uint4 *>(dl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
             }
-            const int off = (q ^ (row & 7)) << 4;   // 128-byte swizzle of 16-byte chunks
-            *reinterpret_cast<uint4 *>(dh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-            *reinterpret_cast<uint4 *>(dl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
           }
           fence_async_shared();
           __syncwarp();
@@ -348,12 +363,15 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
     }
   } else {
     // ------------------------------------------------ epilogue
-    const int quad = warp & 3, row = quad * 32 + lane;
+    // group eg reads the 64-column quarters q with q % 2 == eg (quarters 0 and
+    // 1, which the next unit's first chunks need, are handed back first); group
+    // 0 also keeps the log-sum-exp and writes the posteriors
+    const int quad = warp & 3, row = quad * 32 + lane, eg = (warp - kWEpi0) >> 2;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
     // l_ij scratch of this CTA: [tile parity][component][128 points]
     float *scr = lsc + (size_t)blockIdx.x * 2 * K * kWTile + row;
     // the accumulator starts at zero and is zeroed as it is read: every MMA accumulates
-    for (int q = 0; q < nc; q++) {
+    for (int q = eg; q < nc; q += 2) {
       tmem_zero32(tbase + lane_addr + 64 * q);
       tmem_zero32(tbase + lane_addr + 64 * q + 32);
     }
@@ -361,7 +379,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
     tc_fence_before();
     __syncwarp();
     if (lane == 0)
-      for (int q = 0; q < nc; q++) mbar_arrive(&S.acc_empty[q]);
+      for (int q = eg; q < nc; q += 2) mbar_arrive(&S.acc_empty[q]);
     double lsum = 0.0;
     bool ok = true, have_prev = false;
     int prev_par = 0;
@@ -376,43 +394,50 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       int jmax = 0;
       for (int j = 0; j < K; j++, ui++) {
         float lp = 0.f;
-        if (have_prev && prev_i >= 0) lp = scr[(size_t)(prev_par * K + j) * kWTile];
-        if (!(ok = mbar_wait_warp(&S.acc_full, ui & 1, err))) break;
-        tc_fence_after();
-        const float *bj = wb + (size_t)j * Dp;
-        const float *sj = wsc + (size_t)j * Dp;
-        __half *yj = Y + (size_t)j * Dp * np + (pi >= 0 ? pi : 0);
+        if (eg == 0 && have_prev && prev_i >= 0) lp = scr[(size_t)(prev_par * K + j) * kWTile];
+        ok = mbar_wait_warp(&S.acc_full, ui & 1, err);
         float s4[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int q = 0; q < nc; q++) {
-          uint32_t v[64];
-          tmem_ld64(tbase + lane_addr + 64 * q, v);
-          tmem_wait_ld();
-          tmem_zero32(tbase + lane_addr + 64 * q);
-          tmem_zero32(tbase + lane_addr + 64 * q + 32);
-          tmem_wait_st();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&S.acc_empty[q]);
+        if (ok) {
+          tc_fence_after();
+          const float *bj = wb + (size_t)j * Dp;
+          const float *sj = wsc + (size_t)j * Dp;
+          __half *yj = Y + (size_t)j * Dp * np + (pi >= 0 ? pi : 0);
+          for (int q = eg; q < nc; q += 2) {
+            uint32_t v[64];
+            tmem_ld64(tbase + lane_addr + 64 * q, v);
+            tmem_wait_ld();
+            tmem_zero32(tbase + lane_addr + 64 * q);
+            tmem_zero32(tbase + lane_addr + 64 * q + 32);
+            tmem_wait_st();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.acc_empty[q]);
 #pragma unroll
-          for (int u = 0; u < 16; u++) {
-            const int p0 = 64 * q + 4 * u;
-            const float4 b = __ldg(reinterpret_cast<const float4 *>(bj + p0));
-            const float4 sc = __ldg(reinterpret_cast<const float4 *>(sj + p0));
-            const float y[4] = {fmaf(__uint_as_float(v[4 * u]), sc.x, -b.x),
-                                fmaf(__uint_as_float(v[4 * u + 1]), sc.y, -b.y),
-                                fmaf(__uint_as_float(v[4 * u + 2]), sc.z, -b.z),
-                                fmaf(__uint_as_float(v[4 * u + 3]), sc.w, -b.w)};
+            for (int u = 0; u < 16; u++) {
+              const int p0 = 64 * q + 4 * u;
+              const float4 b = __ldg(reinterpret_cast<const float4 *>(bj + p0));
+              const float4 sc = __ldg(reinterpret_cast<const float4 *>(sj + p0));
+              const float y[4] = {fmaf(__uint_as_float(v[4 * u]), sc.x, -b.x),
+                                  fmaf(__uint_as_float(v[4 * u + 1]), sc.y, -b.y),
+                                  fmaf(__uint_as_float(v[4 * u + 2]), sc.z, -b.z),
+                                  fmaf(__uint_as_float(v[4 * u + 3]), sc.w, -b.w)};
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-              s4[e] = fmaf(y[e], y[e], s4[e]);
-              // output dim k = Dp - 1 - p; |y| beyond the FP16 range only occurs
-              // where the posterior is 0 (the M-step multiplies it by sqrt r = 0)
-              if (pi >= 0)
-                yj[(size_t)(Dp - 1 - (p0 + e)) * np] = __float2half_rn(fminf(fmaxf(y[e], -65504.f), 65504.f));
+              for (int e = 0; e < 4; e++) {
+                s4[e] = fmaf(y[e], y[e], s4[e]);
+                // output dim k = Dp - 1 - p; |y| beyond the FP16 range only occurs
+                // where the posterior is 0 (the M-step multiplies it by sqrt r = 0)
+                if (pi >= 0)
+                  yj[(size_t)(Dp - 1 - (p0 + e)) * np] = __float2half_rn(fminf(fmaxf(y[e], -65504.f), 65504.f));
+              }
             }
           }
         }
-        const float s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        float s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+        if (eg == 1) S.ssum[ui & 1][row] = s;
+        // both groups leave together when a wait gave up
+        if (!(ok = bar_and(2, 256, ok))) break;
+        if (eg == 1) continue;
+        s += S.ssum[ui & 1][row];
         if (have_prev && prev_i >= 0) w_store_post(Rh, Rl, (size_t)j * np + prev_i, expf(lp - prev_lse));
         // c_j carried as float hi + lo
         const float l = (chi[j] - 0.5f * s) + clo[j];
@@ -433,14 +458,16 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       prev_par = par;
       have_prev = true;
     }
-    if (ok && have_prev && prev_i >= 0)
-      for (int j = 0; j < K; j++)
-        w_store_post(Rh, Rl, (size_t)j * np + prev_i, expf(scr[(size_t)(prev_par * K + j) * kWTile] - prev_lse));
+    if (eg == 0) {
+      if (ok && have_prev && prev_i >= 0)
+        for (int j = 0; j < K; j++)
+          w_store_post(Rh, Rl, (size_t)j * np + prev_i, expf(scr[(size_t)(prev_par * K + j) * kWTile] - prev_lse));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-    if (lane == 0) S.red[warp - 6] = lsum;
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    if (threadIdx.x == 192) part[blockIdx.x] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
+      for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+      if (lane == 0) S.red[warp - kWEpi0] = lsum;
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (threadIdx.x == kWEpi0 * 32) part[blockIdx.x] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -545,7 +572,10 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
     const int p = threadIdx.x - 64;   // rows p and p + 128
     uint32_t i = 0;
     bool ok = true;
-    double s0 = 0.0, s1[2] = {0.0, 0.0};
+    // sum r, sum r y and sum z^2 (the diagonal: its increments are all positive,
+    // which the tensor core's truncating accumulation would bias low) of rows
+    // p and p + 128 over the segment
+    double s0 = 0.0, s1[2] = {0.0, 0.0}, s2[2] = {0.0, 0.0};
     for (int64_t f = f0; f < f1 && ok; f++, i++) {
       const int s = i % kVS;
       ok = mbar_wait_warp(&S.in_full[s], (i / kVS) & 1, err);
@@ -561,7 +591,7 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
         const int rw = p + 128 * h;
         if (rw < Dp) {
           uint8_t *rp = reinterpret_cast<uint8_t *>(S.y[s]) + rw * 128;
-          float acc = 0.f;
+          float acc = 0.f, sq = 0.f;
 #pragma unroll
           for (int it = 0; it < 8; it++) {
             const int q = (it + p) & 7;       // consecutive rows start at different banks
@@ -576,10 +606,13 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
               const float2 zf = __half22float2(vh[u]), wf = __half22float2(wh[u]);
               acc = fmaf(zf.x, wf.x, acc);
               acc = fmaf(zf.y, wf.y, acc);
+              sq = fmaf(zf.x, zf.x, sq);
+              sq = fmaf(zf.y, zf.y, sq);
             }
             *reinterpret_cast<uint4 *>(rp + q * 16) = v;
           }
           s1[h] += (double)acc;
+          s2[h] += (double)sq;
         }
       }
       fence_async_shared();
@@ -589,8 +622,10 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
         double *sp = spart + ((size_t)blockIdx.x * nslot + ((int)(f / nbk) - j0)) * kSPart;
         sp[p] = s1[0];
         sp[p + 128] = s1[1];
-        if (p < kVBlk) sp[kWMax + p] = s0;
-        s0 = 0.0, s1[0] = 0.0, s1[1] = 0.0;
+        sp[kWMax + p] = s2[0];
+        sp[kWMax + p + 128] = s2[1];
+        if (p < kVBlk) sp[2 * kWMax + p] = s0;
+        s0 = 0.0, s1[0] = s1[1] = 0.0, s2[0] = s2[1] = 0.0;
       }
     }
   } else {
@@ -668,7 +703,7 @@ k_wide_gather(const double *__restrict__ cpart, const double *__restrict__ spart
   double r = 0.0;
   for (int e = threadIdx.x; e < cnt * kVBlk; e += blockDim.x) {
     const int u = e / kVBlk, t = e - u * kVBlk;
-    r += spart[((size_t)s_cta[u] * nslot + s_slot[u]) * kSPart + kWMax + t];
+    r += spart[((size_t)s_cta[u] * nslot + s_slot[u]) * kSPart + 2 * kWMax + t];
   }
   red[threadIdx.x] = r;
   __syncthreads();
@@ -690,8 +725,12 @@ k_wide_gather(const double *__restrict__ cpart, const double *__restrict__ spart
     if (b > a) continue;
     double v = 0.0;
     for (int u = 0; u < cnt; u++) {
-      const double *cp = cpart + ((size_t)s_cta[u] * nslot + s_slot[u]) * (size_t)ncols * 128;
-      v += (a < 128) ? cp[(size_t)b * 128 + a] : cp[(size_t)(128 + b) * 128 + (a - 128)];
+      if (a == b) {
+        v += spart[((size_t)s_cta[u] * nslot + s_slot[u]) * kSPart + kWMax + a];
+      } else {
+        const double *cp = cpart + ((size_t)s_cta[u] * nslot + s_slot[u]) * (size_t)ncols * 128;
+        v += (a < 128) ? cp[(size_t)b * 128 + a] : cp[(size_t)(128 + b) * 128 + (a - 128)];
+      }
     }
     const double m = v / Nj - ybar[a] * ybar[b];
     M[(size_t)a * d + b] = m;
