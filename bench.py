@@ -364,7 +364,9 @@ def main():
     if est_ms >= cov_ms:
         kern, dom_ms, dom_flops = "k_estep_tc", est_ms, fl["estep"]
     else:
-        kern, dom_ms, dom_flops = "k_cov_tc", cov_ms, fl["cov"]
+        # the z x^T kernel unless FEM_COV_KERNEL=zz selects the z z^T one
+        kern = "k_cov_tc" if os.environ.get("FEM_COV_KERNEL", "").startswith("zz") else "k_cov_zx"
+        dom_ms, dom_flops = cov_ms, fl["cov"]
     achieved = dom_flops / (dom_ms / 1e3) / 1e12
     roof = {"kernel": kern, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "peak_source": peak_src, "traffic": profiled_traffic(kern),
