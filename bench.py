@@ -787,10 +787,10 @@ def run_illcond(args, rank, world, local):
     import torch
     from fastem_gb300 import CudaMatrixEM, GaussianMixture, synth
     from fastem_gb300 import _capi as C
-    X, info = synth.em_illcond()
+    X, info = synth.em_illcond(n=args.n or (1 << 21))
     n, d, k = X.shape[0], X.shape[1], 64
     init = (info["weights"], info["means"] + 0.1, info["covs"] * 1.05)
-    cfg = {"workload": "em_illcond N=2097152 d=256 K=64, one EM sweep per step", "n": n, "d": d, "k": k,
+    cfg = {"workload": "em_illcond N=%d d=256 K=64, one EM sweep per step" % n, "n": n, "d": d, "k": k,
            "init": "generating mixture, means + 0.1, covariances x 1.05", "svd": "off (-S)",
            "reg_coef": ILL_REG, "l2": "inputs larger than L2 (X 2.1 GB, whitened offsets 68.7 GB)"}
     if args.impl == "reference":
@@ -845,7 +845,7 @@ def run_illcond(args, rank, world, local):
             except C.FemError as e:
                 other[prec] = {"status": str(e), "failed_at_sweep": em.GetIterCounter()}
     # accuracy against FP64: 15 sweeps on the first 2^19 rows
-    m = 1 << 19
+    m = min(n, 1 << 19)
     Xs = np.ascontiguousarray(X[:m])
     tr, post = {}, {}
     for prec in ("fp64", "mixed", "fp32"):
