@@ -532,7 +532,10 @@ def run_batched(args, rank, world, local):
     mixtures = [GaussianMixture(*init) for _, init in data]
     packed = np.concatenate([X.reshape(-1) for X, _ in data])
     x_bytes = packed.nbytes
+    from fastem_gb300.batch import TUNING_TABLE, load_tuning
     B = CudaBatchEM(shapes, device=local, max_sweeps=BATCH_SWEEPS)
+    tuning = B.Tuning()
+    tuning_src = ("autotuner table " + os.path.relpath(TUNING_TABLE, ROOT)) if load_tuning() else "library defaults"
     B.SetParameters(BATCH_SWEEPS, 0.0, 1e12)
     B.CopyPacked(packed)
 
@@ -636,7 +639,8 @@ def run_batched(args, rank, world, local):
                    + (", only the d = %d fits" % args.fits_d if args.fits_d else ""),
                    "total_points": int(sum(f["n"] for f in fits)), "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (rows %.2f GB, posteriors %.2f GB)" % (
-                       x_bytes / 1e9, sum(n * k for d, n, k in shapes) * 4 / 1e9)},
+                       x_bytes / 1e9, sum(n * k for d, n, k in shapes) * 4 / 1e9),
+                   "work_items": dict(tuning, source=tuning_src)},
         "phase_ms_per_step": per_step, "class_ms_per_step": per_class,
         "roofline": {"kernel": "k_b_cov<32> (covariance sums, d = 32 fits)", "bound": "fp32", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,

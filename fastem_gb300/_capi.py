@@ -37,7 +37,8 @@ EXPORTS = [
     "fem_em_batch_upload", "fem_em_batch_upload_packed", "fem_em_batch_set_params",
     "fem_em_batch_get_params", "fem_em_batch_train", "fem_em_batch_trace",
     "fem_em_batch_fail_component", "fem_em_batch_timing_enable", "fem_em_batch_timing",
-    "fem_em_batch_timing_classes",
+    "fem_em_batch_timing_classes", "fem_em_batch_tuning_default", "fem_em_batch_create_tuned",
+    "fem_em_batch_get_tuning",
     "fem_km_config_default", "fem_km_create", "fem_km_destroy", "fem_km_upload",
     "fem_km_upload_device", "fem_km_init_data_structures", "fem_km_compute_mse_and_correct",
     "fem_km_correct_without_mse",
@@ -65,6 +66,11 @@ class EmConfig(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("device", ctypes.c_int), ("max_sweeps", ctypes.c_int),
                 ("eps", ctypes.c_double), ("abort_thr", ctypes.c_double),
                 ("reg_coef", ctypes.c_double), ("svd", ctypes.c_int)]
+
+
+class BatchTuning(ctypes.Structure):
+    """fem_em_batch_tuning: points per means / covariance item per dimension class."""
+    _fields_ = [("means_chunk", ctypes.c_int * 4), ("cov_chunk", ctypes.c_int * 4)]
 
 
 class KmConfig(ctypes.Structure):
@@ -124,6 +130,10 @@ def lib():
         "fem_em_batch_timing_enable": ([P, i32], i32),
         "fem_em_batch_timing": ([P, P, P, P], i32),
         "fem_em_batch_timing_classes": ([P, P], i32),
+        "fem_em_batch_tuning_default": ([ctypes.POINTER(BatchTuning)], None),
+        "fem_em_batch_create_tuned": ([i32, P, P, P, ctypes.POINTER(EmConfig), ctypes.POINTER(BatchTuning), pP],
+                                      i32),
+        "fem_em_batch_get_tuning": ([P, ctypes.POINTER(BatchTuning)], i32),
         "fem_km_config_default": ([ctypes.POINTER(KmConfig)], None),
         "fem_km_create": ([i32, i64, i32, ctypes.POINTER(KmConfig), pP], i32),
         "fem_km_destroy": ([P], None),

@@ -9,17 +9,46 @@ Cholesky / condition-number failure.  The difference is the schedule: every
 kernel of a sweep covers all fits still sweeping.
 """
 import ctypes
+import json
+import os
 
 import numpy as np
 
 from . import _capi as C
 from .em import GaussianMixture
 
+# work-item sizes measured by fastem_gb300/autotune.py on a GB300
+TUNING_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "batch_gb300.json")
+CLASS_DIMS = (4, 8, 16, 32)
+
+
+def load_tuning(path=TUNING_TABLE):
+    """{"means_chunk": [4], "cov_chunk": [4]} from an autotuner table, or None
+    when there is no table."""
+    try:
+        with open(path) as f:
+            t = json.load(f)
+    except OSError:
+        return None
+    return {"means_chunk": [int(v) for v in t["means_chunk"]], "cov_chunk": [int(v) for v in t["cov_chunk"]]}
+
+
+def tuning_struct(tuning):
+    t = C.BatchTuning()
+    C.lib().fem_em_batch_tuning_default(ctypes.byref(t))
+    if tuning:
+        for c in range(4):
+            t.means_chunk[c] = int(tuning["means_chunk"][c])
+            t.cov_chunk[c] = int(tuning["cov_chunk"][c])
+    return t
+
 
 class CudaBatchEM:
-    """shapes: sequence of (d, n, k) per fit (d <= 32, k <= 64)."""
+    """shapes: sequence of (d, n, k) per fit (d <= 32, k <= 64).  tuning: "table"
+    (the autotuner's table when present, else the library defaults), None (the
+    library defaults) or {"means_chunk": [4], "cov_chunk": [4]}."""
 
-    def __init__(self, shapes, device=0, max_sweeps=1000000):
+    def __init__(self, shapes, device=0, max_sweeps=1000000, tuning="table"):
         shapes = [(int(d), int(n), int(k)) for d, n, k in shapes]
         self.shapes = shapes
         self.nfits = len(shapes)
@@ -31,13 +60,22 @@ class CudaBatchEM:
         cfg.precision = C.PREC["fp32"]
         cfg.device = device
         cfg.max_sweeps = int(max_sweeps)
+        if isinstance(tuning, str):
+            tuning = load_tuning() if tuning == "table" else load_tuning(tuning)
+        t = tuning_struct(tuning)
         h = ctypes.c_void_p()
-        C.check(C.lib().fem_em_batch_create(self.nfits, C.ptr(d), C.ptr(n), C.ptr(k), ctypes.byref(cfg),
-                                            ctypes.byref(h)))
+        C.check(C.lib().fem_em_batch_create_tuned(self.nfits, C.ptr(d), C.ptr(n), C.ptr(k), ctypes.byref(cfg),
+                                                  ctypes.byref(t), ctypes.byref(h)))
         self._h = h
         self.status = np.zeros(self.nfits, dtype=np.int32)
         self.iters = np.zeros(self.nfits, dtype=np.int32)
         self.logl = np.full(self.nfits, np.nan)
+
+    def Tuning(self):
+        """the work-item sizes this batch was created with"""
+        t = C.BatchTuning()
+        C.check(C.lib().fem_em_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {"means_chunk": list(t.means_chunk), "cov_chunk": list(t.cov_chunk)}
 
     def close(self):
         if getattr(self, "_h", None):

@@ -23,8 +23,9 @@
 // to multiples of 4 floats so the E-step reads it with 16-byte loads.
 //
 // Work items are built on the host when the batch is created (the shapes
-// are fixed): E-step items of 128 P points, means items of kBMChunk points,
-// covariance items of kBCChunk points x one range of <= 256 (component,
+// are fixed): E-step items of 128 P points, means items and covariance items
+// of a per-class number of points (fem_em_batch_tuning; defaults kBMChunk,
+// kBCChunk) x one range of <= 256 (component,
 // TB x TB block) units.  Item lists are grouped by dimension class; each
 // class is one launch per phase.
 #include <algorithm>
@@ -939,6 +940,7 @@ struct fem_em_batch {
   size_t c_smem[kClasses] = {};
   int c_kmax[kClasses] = {};       // largest k of the class's fits
   size_t m_smem[kClasses] = {};     // means kernel dynamic shared memory
+  fem_em_batch_tuning tuning{};     // work-item sizes per class
   std::vector<BState> hstate;
   // timing: phase boundaries of the sweeps since the last host sync
   bool timing = false;
@@ -1103,13 +1105,34 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
 
 }  // namespace
 
+extern "C" void fem_em_batch_tuning_default(fem_em_batch_tuning *t) {
+  if (!t) return;
+  for (int c = 0; c < kClasses; c++) t->means_chunk[c] = kBMChunk, t->cov_chunk[c] = kBCChunk;
+}
+
 extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, const int *k,
                                    const fem_em_config *cfg, fem_em_batch **out) {
+  return fem_em_batch_create_tuned(nfits, d, n, k, cfg, nullptr, out);
+}
+
+extern "C" int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t *n, const int *k,
+                                         const fem_em_config *cfg, const fem_em_batch_tuning *tuning,
+                                         fem_em_batch **out) {
   if (!out || nfits < 1 || !d || !n || !k) {
     set_error("fem_em_batch_create: bad arguments");
     return FEM_ERR_BAD_ARG;
   }
   *out = nullptr;
+  fem_em_batch_tuning tune;
+  fem_em_batch_tuning_default(&tune);
+  if (tuning) tune = *tuning;
+  for (int c = 0; c < kClasses; c++) {
+    const int a = tune.means_chunk[c], v = tune.cov_chunk[c];
+    if (a < 256 || a > 16384 || a % 128 || v < 256 || v > 16384 || v % 128) {
+      set_error("tuning: class %d item sizes must be multiples of 128 in [256, 16384] (means %d, cov %d)", c, a, v);
+      return FEM_ERR_BAD_ARG;
+    }
+  }
   fem_em_config c;
   if (cfg) c = *cfg;
   else {
@@ -1143,6 +1166,7 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
   }
   b->nfits = nfits;
   b->cfg = c;
+  b->tuning = tune;
   b->hfits.resize(nfits);
   b->have_data.assign(nfits, 0);
   b->have_params.assign(nfits, 0);
@@ -1215,8 +1239,9 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
       F.e_count = (int)ei.size() - F.e_first;
       F.m_first = (int)mi.size();
       F.m_part = mp;
-      for (int64_t p = 0; p < F.n; p += kBMChunk) {
-        mi.push_back(MItem{f, (int)p, (int)std::min<int64_t>(F.n, p + kBMChunk), mp});
+      const int mch = tune.means_chunk[c], cch = tune.cov_chunk[c];
+      for (int64_t p = 0; p < F.n; p += mch) {
+        mi.push_back(MItem{f, (int)p, (int)std::min<int64_t>(F.n, p + mch), mp});
         mp += (int64_t)F.k * (F.D + 4);
       }
       F.m_count = (int)mi.size() - F.m_first;
@@ -1229,12 +1254,12 @@ extern "C" int fem_em_batch_create(int nfits, const int *d, const int64_t *n, co
         F.c_stride += (int64_t)ng * (u1 - u0) * per;
       }
       F.c_chunks = 0;
-      for (int64_t p = 0; p < F.n; p += kBCChunk) {
+      for (int64_t p = 0; p < F.n; p += cch) {
         int64_t off = cp;
         for (int ug = 0; ug < F.nug; ug++) {
           int u0, u1, ng, per;
           unit_range(F.k, F.D, ug, &u0, &u1, &ng, &per);
-          ci.push_back(CItem{f, (int)p, (int)std::min<int64_t>(F.n, p + kBCChunk), u0, u1, off});
+          ci.push_back(CItem{f, (int)p, (int)std::min<int64_t>(F.n, p + cch), u0, u1, off});
           off += (int64_t)ng * (u1 - u0) * per;
         }
         cp += F.c_stride;
@@ -1474,6 +1499,16 @@ extern "C" int fem_em_batch_fail_component(fem_em_batch *b, int fit, int *compon
     return FEM_ERR_BAD_ARG;
   }
   *component = b->hstate[fit].fail_comp;
+  return FEM_OK;
+}
+
+extern "C" int fem_em_batch_get_tuning(fem_em_batch *b, fem_em_batch_tuning *t) {
+  FEM_TRY(check_batch(b));
+  if (!t) {
+    set_error("null output");
+    return FEM_ERR_BAD_ARG;
+  }
+  *t = b->tuning;
   return FEM_OK;
 }
 

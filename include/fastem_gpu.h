@@ -173,6 +173,22 @@ typedef struct fem_em_batch fem_em_batch;
 
 int fem_em_batch_create(int nfits, const int *d, const int64_t *n, const int *k,
                         const fem_em_config *cfg, fem_em_batch **out);
+/* Work-item sizes per dimension class (d <= 4, 8, 16, 32): points per means
+ * item and per covariance item (multiples of 128 in [256, 16384]).  The
+ * engine has no reference counterpart; the sizes change the schedule and the
+ * order of the FP32 item sums, not the sweep.  fastem_gb300/autotune.py
+ * measures them on a GPU and writes the table that CudaBatchEM loads. */
+typedef struct {
+  int means_chunk[4];
+  int cov_chunk[4];
+} fem_em_batch_tuning;
+void fem_em_batch_tuning_default(fem_em_batch_tuning *t);
+/* fem_em_batch_create with the item sizes of `tuning` (NULL: the defaults) */
+int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t *n, const int *k,
+                              const fem_em_config *cfg, const fem_em_batch_tuning *tuning,
+                              fem_em_batch **out);
+/* the item sizes a batch was created with */
+int fem_em_batch_get_tuning(fem_em_batch *b, fem_em_batch_tuning *t);
 void fem_em_batch_destroy(fem_em_batch *b);
 /* EMAlgorithm::SetParameters (EM2/EMAlgorithm.cpp:25-30), for every fit */
 int fem_em_batch_set_parameters(fem_em_batch *b, int max_sweeps, double eps, double abort_thr,

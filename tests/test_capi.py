@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -82,3 +83,39 @@ def test_python_binding_raises_when_library_missing(monkeypatch, tmp_path):
     monkeypatch.setattr(_capi, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(ImportError):
         _capi.lib()
+
+
+def test_batch_tuning_defaults_and_bad_sizes_rejected(gpu_lib):
+    """the default work-item sizes, and sizes outside [256, 16384] or not
+    multiples of 128 refused before any device call"""
+    import ctypes
+    from fastem_gb300 import _capi as C
+    t = C.BatchTuning()
+    C.lib().fem_em_batch_tuning_default(ctypes.byref(t))
+    assert list(t.means_chunk) == [2048] * 4 and list(t.cov_chunk) == [4096] * 4
+    d = np.array([8], dtype=np.int32)
+    n = np.array([1000], dtype=np.int64)
+    k = np.array([3], dtype=np.int32)
+    cfg = C.EmConfig()
+    C.lib().fem_em_config_default(ctypes.byref(cfg))
+    cfg.precision = C.PREC["fp32"]
+    for bad in (100, 200, 32768, 1000):
+        t.means_chunk[2] = bad
+        h = ctypes.c_void_p()
+        st = C.lib().fem_em_batch_create_tuned(1, C.ptr(d), C.ptr(n), C.ptr(k), ctypes.byref(cfg), ctypes.byref(t),
+                                               ctypes.byref(h))
+        assert st == C.FEM_ERR_BAD_ARG and not h.value
+        assert b"multiples of 128" in C.lib().fem_last_error()
+    t.means_chunk[2] = 2048
+
+
+def test_batch_tuning_table_is_valid():
+    """the autotuner's committed table holds item sizes the engine accepts"""
+    from fastem_gb300.batch import TUNING_TABLE, load_tuning
+    import os
+    if not os.path.exists(TUNING_TABLE):
+        pytest.skip("no autotuner table")
+    t = load_tuning()
+    for key in ("means_chunk", "cov_chunk"):
+        assert len(t[key]) == 4
+        assert all(256 <= v <= 16384 and v % 128 == 0 for v in t[key])

@@ -25,9 +25,9 @@ def fits(shapes=SHAPES, seed_shift=0):
     return out
 
 
-def train_batch(data, sweeps, eps=0.0, abort_thr=1e12, reg=0.0, svd=False):
+def train_batch(data, sweeps, eps=0.0, abort_thr=1e12, reg=0.0, svd=False, tuning="table"):
     shapes = [(X.shape[1], X.shape[0], len(init[0])) for X, init in data]
-    with CudaBatchEM(shapes) as B:
+    with CudaBatchEM(shapes, tuning=tuning) as B:
         B.SetParameters(sweeps, eps, abort_thr, reg)
         st, it, ll = B.Train([X for X, _ in data], [GaussianMixture(*init) for _, init in data], svd=svd)
         traces = [B.Trace(i) for i in range(len(data))]
@@ -36,12 +36,19 @@ def train_batch(data, sweeps, eps=0.0, abort_thr=1e12, reg=0.0, svd=False):
     return dict(status=st, iters=it, logl=ll, traces=traces, mix=mix, fail=fail)
 
 
-def test_batch_matches_oracle(gpu_lib, oracle):
+# item sizes: the library defaults, the smallest and the largest the autotuner
+# tries, and its committed table
+TUNINGS = {"default": None, "small": {"means_chunk": [512] * 4, "cov_chunk": [1024] * 4},
+           "large": {"means_chunk": [8192] * 4, "cov_chunk": [8192] * 4}, "table": "table"}
+
+
+@pytest.mark.parametrize("tuning", list(TUNINGS))
+def test_batch_matches_oracle(gpu_lib, oracle, tuning):
     """10 sweeps of every fit: |dlogL/N| <= 1e-5 per sweep against the FP64
     oracle (FP32 per-point terms, FP64 sums), same IterCounter, means and
-    weights close."""
+    weights close -- whatever the work-item sizes."""
     data = fits()
-    got = train_batch(data, 10)
+    got = train_batch(data, 10, tuning=TUNINGS[tuning])
     for i, (X, init) in enumerate(data):
         ref = oracle.em_train(X, *init, 10, eps=0.0, abort_thr=1e12)
         assert ref["status"] == 0
