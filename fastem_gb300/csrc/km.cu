@@ -36,52 +36,53 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // ----------------------------------------------------------- data stats
-// per-block column sums (FP64) and max |x|
+// One pass over X for the data mean g, max |x| and sum_i ||x_i - g||^2: per
+// CTA and column, S1 = sum t and S2 = sum t^2 in FP64 with t = x - c (c = the
+// dataset's first row: x - c is exact in FP64 for FP32 data, and c lies inside
+// the data, so S2 - S1^2 / n below does not cancel), plus max |x|.  The host
+// merges the CTAs: g = c + S1 / n, sum ||x - g||^2 = sum_q (S2_q - S1_q^2 / n).
+// Threads own (row group, column) pairs, so a warp reads whole rows.
 __global__ void __launch_bounds__(256)
-k_km_colstats(const float *__restrict__ X, int64_t n, int d, int64_t rows_per_block,
-              double *__restrict__ sums, float *__restrict__ amax) {
-  __shared__ float sm[256];
-  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
+k_km_stats(const float *__restrict__ X, int64_t n, int d, int64_t rows_per_block, const float *__restrict__ c,
+           double *__restrict__ s1, double *__restrict__ s2, float *__restrict__ amax) {
+  __shared__ double r1[256], r2[256];
+  __shared__ float rm[256];
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block, r1e = min(n, r0 + rows_per_block);
+  const bool narrow = d <= 256;
+  const int groups = narrow ? 256 / d : 1;       // row groups a pass covers
+  const int tid = threadIdx.x;
   float mx = 0.f;
-  for (int q = threadIdx.x; q < d; q += 256) {
-    double s = 0.0;
-    for (int64_t i = r0; i < r1; i++) {
-      const float v = X[i * d + q];
-      s += (double)v;
-      mx = fmaxf(mx, fabsf(v));
+  for (int q0 = 0; q0 < d; q0 += 256) {
+    const int q = q0 + (narrow ? tid % d : tid), g = narrow ? tid / d : 0;
+    const int cols = narrow ? d : min(256, d - q0);
+    double a = 0.0, b = 0.0;
+    if (g < groups && q < d) {
+      const double cq = (double)c[q];
+      for (int64_t i = r0 + g; i < r1e; i += groups) {
+        const float x = X[i * d + q];
+        const double t = (double)x - cq;
+        a += t;
+        b = fma(t, t, b);
+        mx = fmaxf(mx, fabsf(x));
+      }
     }
-    sums[(size_t)blockIdx.x * d + q] = s;
+    r1[tid] = a, r2[tid] = b;
+    __syncthreads();
+    // column q0 + tid's row groups sit at tid + cols g: summed in group order
+    if (tid < cols) {
+      double sa = 0.0, sb = 0.0;
+      for (int gg = 0; gg < groups; gg++) sa += r1[tid + gg * cols], sb += r2[tid + gg * cols];
+      s1[(size_t)blockIdx.x * d + q0 + tid] = sa;
+      s2[(size_t)blockIdx.x * d + q0 + tid] = sb;
+    }
+    __syncthreads();
   }
-  sm[threadIdx.x] = mx;
+  rm[tid] = mx;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     float m = 0.f;
-    for (int t = 0; t < 256; t++) m = fmaxf(m, sm[t]);
+    for (int t = 0; t < 256; t++) m = fmaxf(m, rm[t]);
     amax[blockIdx.x] = m;
-  }
-}
-
-// per-block sum_i ||x_i - g||^2 and sum of (x_i*2^shift) overflow guard not needed
-__global__ void __launch_bounds__(256)
-k_km_x2(const float *__restrict__ X, int64_t n, int d, const double *__restrict__ g,
-        double *__restrict__ part) {
-  __shared__ double red[8];
-  double v = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
-    double s = 0.0;
-    for (int q = 0; q < d; q++) {
-      const double t = (double)X[i * d + q] - g[q];
-      s += t * t;
-    }
-    v += s;
-  }
-  v = warp_sum_d(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int w = 0; w < 8; w++) s += red[w];
-    part[blockIdx.x] = s;
   }
 }
 
@@ -343,20 +344,30 @@ int upload_km(fem_km *h, const float *X, int64_t ld, cudaMemcpyKind kind) {
   FEM_CUDA(cudaSetDevice(h->cfg.device));
   FEM_CUDA(cudaMemcpy2DAsync(h->X, (size_t)d * 4, X, (size_t)ld * 4, (size_t)d * 4, (size_t)n, kind,
                              h->stream));
-  // data mean, max |x| -> fixed-point shift, sum ||x - g||^2
-  const int G = (int)std::min<int64_t>(1024, (n + 1023) / 1024);
+  // data mean, max |x| -> fixed-point shift, sum ||x - g||^2, in one pass
+  const int G = (int)std::min<int64_t>(4 * (int64_t)sm_count(), (n + 255) / 256);
   const int64_t rpb = (n + G - 1) / G;
-  double *sums = nullptr;
+  std::vector<float> c(d);
+  FEM_CUDA(cudaMemcpyAsync(c.data(), h->X, (size_t)d * 4, cudaMemcpyDeviceToHost, h->stream));
+  FEM_CUDA(cudaStreamSynchronize(h->stream));
+  float *dc = nullptr;
+  double *s1 = nullptr, *s2 = nullptr;
   float *amax = nullptr;
-  FEM_TRY(dalloc(&sums, (size_t)G * d));
+  FEM_TRY(dalloc(&dc, d));
+  FEM_TRY(dalloc(&s1, (size_t)G * d));
+  FEM_TRY(dalloc(&s2, (size_t)G * d));
   FEM_TRY(dalloc(&amax, G));
-  k_km_colstats<<<G, 256, 0, h->stream>>>(h->X, n, d, rpb, sums, amax);
-  std::vector<double> hs((size_t)G * d);
+  FEM_CUDA(cudaMemcpyAsync(dc, c.data(), (size_t)d * 4, cudaMemcpyHostToDevice, h->stream));
+  k_km_stats<<<G, 256, 0, h->stream>>>(h->X, n, d, rpb, dc, s1, s2, amax);
+  std::vector<double> h1((size_t)G * d), h2((size_t)G * d);
   std::vector<float> hm(G);
-  cudaMemcpyAsync(hs.data(), sums, hs.size() * 8, cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(h1.data(), s1, h1.size() * 8, cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(h2.data(), s2, h2.size() * 8, cudaMemcpyDeviceToHost, h->stream);
   cudaMemcpyAsync(hm.data(), amax, hm.size() * 4, cudaMemcpyDeviceToHost, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
-  dfree(sums);
+  dfree(dc);
+  dfree(s1);
+  dfree(s2);
   dfree(amax);
   if (e != cudaSuccess) {
     set_error("dataset statistics failed: %s", cudaGetErrorString(e));
@@ -364,28 +375,17 @@ int upload_km(fem_km *h, const float *X, int64_t ld, cudaMemcpyKind kind) {
   }
   float mx = 0.f;
   for (int b = 0; b < G; b++) mx = std::max(mx, hm[b]);
+  h->xg2 = 0.0;
   for (int q = 0; q < d; q++) {
-    double s = 0.0;
-    for (int b = 0; b < G; b++) s += hs[(size_t)b * d + q];
-    h->hg[q] = s / (double)n;
+    double a = 0.0, b2 = 0.0;
+    for (int b = 0; b < G; b++) a += h1[(size_t)b * d + q], b2 += h2[(size_t)b * d + q];
+    h->hg[q] = (double)c[q] + a / (double)n;
+    h->xg2 += b2 - a * a / (double)n;
   }
   // |x| * 2^shift * n < 2^62: the per-CTA and the final int64 sums cannot overflow
   const double lg = std::log2((double)std::max(mx, 1e-30f)) + std::log2((double)n);
   h->shift = (int)std::min(40.0, std::floor(61.0 - std::ceil(lg)));
   FEM_CUDA(cudaMemcpyAsync(h->g, h->hg, d * 8, cudaMemcpyHostToDevice, h->stream));
-  double *part = nullptr;
-  FEM_TRY(dalloc(&part, 1024));
-  k_km_x2<<<1024, 256, 0, h->stream>>>(h->X, n, d, h->g, part);
-  std::vector<double> hp(1024);
-  cudaMemcpyAsync(hp.data(), part, 1024 * 8, cudaMemcpyDeviceToHost, h->stream);
-  e = cudaStreamSynchronize(h->stream);
-  dfree(part);
-  if (e != cudaSuccess) {
-    set_error("dataset statistics failed: %s", cudaGetErrorString(e));
-    return FEM_ERR_CUDA;
-  }
-  h->xg2 = 0.0;
-  for (double v : hp) h->xg2 += v;
   h->have_data = true;
   return FEM_OK;
 }
