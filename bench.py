@@ -476,11 +476,11 @@ def batched_workload():
     return fits, data
 
 
-def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None):
+def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None, mixed_traces=None):
     """The oracle's TrainNoCopy (FP64, OpenMP over all host cores) on every
     `sample_every`-th fit, 30 sweeps each.  With `gpu_traces` ({fit: LogL
     trace}) the oracle's traces of the same fits check the GPU's:
-    the largest per-fit |dlogL/N|."""
+    the largest per-fit |dlogL/N| (and the same for `mixed_traces`)."""
     from oracle import oracle as O
     O.lib()
     idx = list(range(0, len(fits), sample_every))
@@ -490,16 +490,20 @@ def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None):
         X, init = data[i]
         refs[i] = O.em_train(X, *init, BATCH_SWEEPS, eps=0.0, abort_thr=1e12, nthreads=os.cpu_count())
     dt = time.perf_counter() - t0
-    errs = []
-    for i, tr in (gpu_traces or {}).items():
-        ref = refs.get(i)
-        if ref is not None and ref["status"] == 0:
-            m = min(len(tr), len(ref["logl"]))
-            errs.append(float(np.max(np.abs(tr[:m] - ref["logl"][:m])) / fits[i]["n"]))
+    def worst(traces):
+        errs = []
+        for i, tr in (traces or {}).items():
+            ref = refs.get(i)
+            if ref is not None and ref["status"] == 0 and tr is not None:
+                m = min(len(tr), len(ref["logl"]))
+                errs.append(float(np.max(np.abs(tr[:m] - ref["logl"][:m])) / fits[i]["n"]))
+        return errs
+    errs, merrs = worst(gpu_traces), worst(mixed_traces)
     return {"value": len(idx) / dt, "unit": "fits/s", "cores": os.cpu_count(), "kind": "port",
             "sample": "%d of the %d fits (every %dth), %d sweeps each, %.1f s" % (len(idx), len(fits), sample_every,
                                                                                  BATCH_SWEEPS, dt),
-            "max_dlogL_per_N_vs_gpu": max(errs) if errs else None, "checked_fits": len(errs)}
+            "max_dlogL_per_N_vs_gpu": max(errs) if errs else None, "checked_fits": len(errs),
+            "max_dlogL_per_N_vs_mixed_per_fit": max(merrs) if merrs else None, "checked_mixed_fits": len(merrs)}
 
 
 def run_batched(args, rank, world, local):
@@ -580,34 +584,46 @@ def run_batched(args, rank, world, local):
         dt = dist.max(time.perf_counter() - t0)
         e2e = {"value": world * nf * steps / dt, "unit": "fits/s", "h2d_bytes_per_step": x_bytes + p_bytes,
                "d2h_bytes_per_step": p_bytes + nf * 16}
-    # the previous scheme: one FP32 handle and stream per fit, 16 host threads
-    per_fit = None
+    # one handle and stream per fit, 16 host threads: the FP32 form (the scheme
+    # the batched engine replaced) and the mixed tensor-core form (the single-fit
+    # tcgen05 kernels, d zero-padded to 64; not batched into one launch)
+    per_fit, per_fit_mixed, mixed_traces = None, None, {}
     if not args.no_fp32:
         import concurrent.futures as cf
 
-        def run(i):
+        def run(i, prec):
             X, init = data[i]
             d, n, k = shapes[i]
-            with CudaMatrixEM(d, n, k, precision="fp32", device=local) as em:
+            with CudaMatrixEM(d, n, k, precision=prec, device=local) as em:
                 em.SetParameters(BATCH_SWEEPS, 0.0, 1e12)
                 try:
                     em.Train(X, GaussianMixture(*init))
                 except Exception:
                     return None
-                return em.logl_trace
-        with cf.ThreadPoolExecutor(16) as ex:
-            list(ex.map(run, range(8)))
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            list(ex.map(run, range(nf)))
-            torch.cuda.synchronize()
-            per_fit = {"value": nf / (time.perf_counter() - t0), "unit": "fits/s",
-                       "scheme": "one FP32 handle and stream per fit, 16 host threads"}
+                return em.logl_trace.copy()
+        for prec in ("fp32", "mixed"):
+            with cf.ThreadPoolExecutor(16) as ex:
+                list(ex.map(lambda i: run(i, prec), range(8)))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                tr = list(ex.map(lambda i: run(i, prec), range(nf)))
+                torch.cuda.synchronize()
+                leg = {"value": nf / (time.perf_counter() - t0), "unit": "fits/s",
+                       "scheme": "one %s handle and stream per fit, 16 host threads" % prec,
+                       "failed_fits": int(sum(t is None for t in tr))}
+            if prec == "fp32":
+                per_fit = leg
+            else:
+                per_fit_mixed = leg
+                mixed_traces = {i: tr[i] for i in range(0, nf, 32)}
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         # the CPU baseline leg also checks the sampled fits' LogL traces
         traces = {i: B.Trace(i)[0] for i in range(0, nf, 32) if st[i] == 0}
-        cpu = batched_cpu_baseline(fits, data, gpu_traces=traces)
+        cpu = batched_cpu_baseline(fits, data, gpu_traces=traces, mixed_traces=mixed_traces)
+        if per_fit_mixed is not None:
+            per_fit_mixed["max_dlogL_per_N_sampled"] = cpu["max_dlogL_per_N_vs_mixed_per_fit"]
+            per_fit_mixed["sampled_fits"] = cpu["checked_mixed_fits"]
     B.close()
     dist.close()
     if rank != 0:
@@ -652,6 +668,7 @@ def run_batched(args, rank, world, local):
         "max_dlogL_per_N_sampled": cpu["max_dlogL_per_N_vs_gpu"] if cpu else None,
         "sampled_fits": cpu["checked_fits"] if cpu else 0,
         "per_fit_handles": per_fit, "speedup_vs_per_fit_handles": (value / per_fit["value"]) if per_fit else None,
+        "mixed_per_fit_handles": per_fit_mixed,
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": tm["launches"],
     }
     print(json.dumps(line), flush=True)
