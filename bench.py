@@ -476,11 +476,12 @@ def batched_workload():
     return fits, data
 
 
-def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None, mixed_traces=None):
+def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None, mixed_traces=None, extra=None):
     """The oracle's TrainNoCopy (FP64, OpenMP over all host cores) on every
     `sample_every`-th fit, 30 sweeps each.  With `gpu_traces` ({fit: LogL
     trace}) the oracle's traces of the same fits check the GPU's:
-    the largest per-fit |dlogL/N| (and the same for `mixed_traces`)."""
+    the largest per-fit |dlogL/N| (and the same for `mixed_traces` and for
+    each {name: traces} of `extra`)."""
     from oracle import oracle as O
     O.lib()
     idx = list(range(0, len(fits), sample_every))
@@ -499,11 +500,15 @@ def batched_cpu_baseline(fits, data, sample_every=32, gpu_traces=None, mixed_tra
                 errs.append(float(np.max(np.abs(tr[:m] - ref["logl"][:m])) / fits[i]["n"]))
         return errs
     errs, merrs = worst(gpu_traces), worst(mixed_traces)
-    return {"value": len(idx) / dt, "unit": "fits/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d of the %d fits (every %dth), %d sweeps each, %.1f s" % (len(idx), len(fits), sample_every,
-                                                                                 BATCH_SWEEPS, dt),
-            "max_dlogL_per_N_vs_gpu": max(errs) if errs else None, "checked_fits": len(errs),
-            "max_dlogL_per_N_vs_mixed_per_fit": max(merrs) if merrs else None, "checked_mixed_fits": len(merrs)}
+    out = {"value": len(idx) / dt, "unit": "fits/s", "cores": os.cpu_count(), "kind": "port",
+           "sample": "%d of the %d fits (every %dth), %d sweeps each, %.1f s" % (len(idx), len(fits), sample_every,
+                                                                                BATCH_SWEEPS, dt),
+           "max_dlogL_per_N_vs_gpu": max(errs) if errs else None, "checked_fits": len(errs),
+           "max_dlogL_per_N_vs_mixed_per_fit": max(merrs) if merrs else None, "checked_mixed_fits": len(merrs)}
+    for name, traces in (extra or {}).items():
+        e = worst(traces)
+        out["max_dlogL_per_N_vs_" + name] = max(e) if e else None
+    return out
 
 
 def run_batched(args, rank, world, local):
@@ -566,6 +571,32 @@ def run_batched(args, rank, world, local):
     tm = B.Timing()
     ms = dist.max(total * 1e3) / args.steps
     value = world * nf / (ms / 1e3)
+    # the mixed form of the engine: the E-step of the d > 16 fits on the tensor cores
+    mixed = None
+    mixed_traces_batched = {}
+    with CudaBatchEM(shapes, device=local, max_sweeps=BATCH_SWEEPS, precision="mixed") as BM:
+        BM.SetParameters(BATCH_SWEEPS, 0.0, 1e12)
+        BM.CopyPacked(packed)
+        for _ in range(args.warmup):
+            for i, G in enumerate(mixtures):
+                BM.SetMixture(i, G)
+            BM.TrainNoCopy()
+        BM.EnableTiming(True)
+        mtot = 0.0
+        for _ in range(args.steps):
+            for i, G in enumerate(mixtures):
+                BM.SetMixture(i, G)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mst, _, _ = BM.TrainNoCopy()
+            mtot += time.perf_counter() - t0
+        mtm = BM.Timing()
+        mms = dist.max(mtot * 1e3) / args.steps
+        mixed_traces_batched = {i: BM.Trace(i)[0] for i in range(0, nf, 32) if mst[i] == 0}
+        mixed = {"value": world * nf / (mms / 1e3), "unit": "fits/s", "ms_per_step": mms,
+                 "failed_fits": int((mst != 0).sum()),
+                 "estep_ms_d32_per_step": mtm["classes"][32]["estep_ms"] / args.steps,
+                 "estep_ms_d32_per_step_fp32": tm["classes"][32]["estep_ms"] / args.steps}
     # end to end through the C-ABI: pinned host rows -> device, initial mixtures,
     # train, every fit's trained mixture and status back to the host
     e2e = None
@@ -620,7 +651,10 @@ def run_batched(args, rank, world, local):
     if not args.no_cpu and rank == 0 and world == 1:
         # the CPU baseline leg also checks the sampled fits' LogL traces
         traces = {i: B.Trace(i)[0] for i in range(0, nf, 32) if st[i] == 0}
-        cpu = batched_cpu_baseline(fits, data, gpu_traces=traces, mixed_traces=mixed_traces)
+        cpu = batched_cpu_baseline(fits, data, gpu_traces=traces, mixed_traces=mixed_traces,
+                                   extra={"mixed_batched": mixed_traces_batched})
+        if mixed is not None:
+            mixed["max_dlogL_per_N_sampled"] = cpu["max_dlogL_per_N_vs_mixed_batched"]
         if per_fit_mixed is not None:
             per_fit_mixed["max_dlogL_per_N_sampled"] = cpu["max_dlogL_per_N_vs_mixed_per_fit"]
             per_fit_mixed["sampled_fits"] = cpu["checked_mixed_fits"]
@@ -669,6 +703,7 @@ def run_batched(args, rank, world, local):
         "sampled_fits": cpu["checked_fits"] if cpu else 0,
         "per_fit_handles": per_fit, "speedup_vs_per_fit_handles": (value / per_fit["value"]) if per_fit else None,
         "mixed_per_fit_handles": per_fit_mixed,
+        "mixed": mixed,
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": tm["launches"],
     }
     print(json.dumps(line), flush=True)

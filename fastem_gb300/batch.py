@@ -2,8 +2,9 @@
 (fem_em_batch_* in include/fastem_gpu.h).
 
 There is no single reference counterpart -- the reference trains one mixture
-per em2 run -- so each fit here behaves as CudaMatrixEM.Train (precision
-"fp32") would for that fit alone: EMAlgorithm::TrainNoCopy
+per em2 run -- so each fit here behaves as CudaMatrixEM.Train would for that
+fit alone (precision "fp32"; "mixed" runs the E-step of the fits with
+16 < d <= 32 on the tensor cores): EMAlgorithm::TrainNoCopy
 (EM2/EMAlgorithm.cpp:139-191) with its own convergence test, IterCounter and
 Cholesky / condition-number failure.  The difference is the schedule: every
 kernel of a sweep covers all fits still sweeping.
@@ -46,9 +47,11 @@ def tuning_struct(tuning):
 class CudaBatchEM:
     """shapes: sequence of (d, n, k) per fit (d <= 32, k <= 64).  tuning: "table"
     (the autotuner's table when present, else the library defaults), None (the
-    library defaults) or {"means_chunk": [4], "cov_chunk": [4]}."""
+    library defaults) or {"means_chunk": [4], "cov_chunk": [4]}.  precision:
+    "fp32" (CUDA cores) or "mixed" (the E-step of the fits with 16 < d <= 32 on
+    the tensor cores in FP16 x 3 split products, everything else as "fp32")."""
 
-    def __init__(self, shapes, device=0, max_sweeps=1000000, tuning="table"):
+    def __init__(self, shapes, device=0, max_sweeps=1000000, tuning="table", precision="fp32"):
         shapes = [(int(d), int(n), int(k)) for d, n, k in shapes]
         self.shapes = shapes
         self.nfits = len(shapes)
@@ -57,7 +60,7 @@ class CudaBatchEM:
         k = np.array([s[2] for s in shapes], dtype=np.int32)
         cfg = C.EmConfig()
         C.lib().fem_em_config_default(ctypes.byref(cfg))
-        cfg.precision = C.PREC["fp32"]
+        cfg.precision = C.PREC[precision]
         cfg.device = device
         cfg.max_sweeps = int(max_sweeps)
         if isinstance(tuning, str):

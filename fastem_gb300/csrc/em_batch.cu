@@ -36,8 +36,12 @@
 #include <new>
 #include <vector>
 
+#include <cuda.h>
+#include <cuda_fp16.h>
+
 #include "em_factor.cuh"
 #include "fem_internal.cuh"
+#include "tc_ptx.cuh"
 
 namespace fem {
 namespace {
@@ -89,6 +93,8 @@ struct BFit {
   int64_t c_stride;
   double *pi, *mu, *sigma, *psum, *logc;   // k, k d, k d d, k, k
   float *muT, *WT, *logcT;                 // k D, k tri(D), k
+  int64_t xrow;          // mixed form, d <= 32 class: first row in the FP16 split copies (-1: none)
+  int wg;                // first 4-component W group of the tensor-core E-step
 };
 
 // per-fit training state
@@ -911,6 +917,257 @@ k_b_sweep_end(BState *__restrict__ state, int nfits, int it, int max_sweeps, dou
   if (threadIdx.x == 0) *nactive = (int)total;
 }
 
+
+// ================================================ mixed form: tensor-core E-step
+// For the d <= 32 class of a batch created with FEM_PREC_MIXED, the E-step of
+// each 512-point item runs on the tensor cores: four 128-point tiles, each
+// against the fit's components in groups of 4 (128 accumulator columns), in
+// FP16 x 3 split products (x_h W_l, x_l W_h, x_h W_h) with FP32 accumulation,
+// as the single-fit E-step (em_tc.cu) does at d <= 64.  Rows are zero-padded
+// to 64 FP16 columns (128-byte swizzled operand rows); a group's 128 W rows are
+// ordered [outputs 16..31 of its 4 components | outputs 0..15], so the second
+// 16-wide k-step (inputs 16..31, lower triangle) needs only the first 64.
+// The epilogue writes the same FP32 posteriors and per-item LogL partials as
+// k_b_estep, so the rest of the sweep is unchanged.
+constexpr int kTT = 128;            // points per tile
+constexpr int kTWS = 4;             // W group ring
+constexpr int kTThreads = 192;      // warp 0 TMA, 1 MMA, 2..5 epilogue
+constexpr int kTClass = 3;          // the d <= 32 class
+struct __align__(1024) BTSmem {
+  __half xh[2][kTT * 64], xl[2][kTT * 64];
+  __half wh[kTWS][128 * 64], wl[kTWS][128 * 64];
+  uint64_t x_full[2], x_empty[2], w_full[kTWS], w_empty[kTWS], acc_full[2], acc_empty[2], mma_done;
+  uint32_t tmem_base;
+  double red[2][4];
+};
+static_assert(sizeof(BTSmem) + 1024 <= 232448, "batched tensor-core E-step shared memory");
+
+// x -> FP16 hi / lo, rows padded to 64 columns; blockIdx.y = the class's fit
+__global__ void k_bt_split(const BFit *__restrict__ fits, const int *__restrict__ tfits, __half *__restrict__ Xh,
+                           __half *__restrict__ Xl) {
+  const BFit &F = fits[tfits[blockIdx.y]];
+  const int64_t tot = F.n * 64;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e >> 6;
+    const int c = (int)(e & 63);
+    const float x = c < F.d ? F.X[i * F.d + c] : 0.f;
+    const __half h = __float2half_rn(x);
+    Xh[(F.xrow + i) * 64 + c] = h;
+    Xl[(F.xrow + i) * 64 + c] = __float2half_rn(x - __half2float(h));
+  }
+}
+
+// per 4-component group: W = L^-1 (from the FP32 factor) as FP16 hi / lo in
+// the tile order above, b = W mu (FP64 sum), log coefficients as float hi + lo
+// (-inf for padding components)
+__global__ void __launch_bounds__(128)
+k_bt_prep(const BFit *__restrict__ fits, const int2 *__restrict__ tgroups, __half *__restrict__ Wh,
+          __half *__restrict__ Wl, float *__restrict__ bias, float *__restrict__ chi, float *__restrict__ clo) {
+  const int2 fg = tgroups[blockIdx.x];
+  const BFit &F = fits[fg.x];
+  const int r = threadIdx.x, grp = F.wg + fg.y;
+  const int h = r >> 6, q = (r & 63) >> 4, t = r & 15;
+  const int k = h == 0 ? 16 + t : t, j = 4 * fg.y + q;
+  const bool live = j < F.k && k < F.d;
+  constexpr int TRI = tri_off(32);
+  const float *w = F.WT + (size_t)j * TRI + tri_off(k);
+  double bsum = 0.0;
+  for (int e = 0; e < 64; e++) {
+    const float v = (live && e <= k && e < F.d) ? w[e] : 0.f;
+    const __half vh = __float2half_rn(v);
+    Wh[((size_t)grp * 128 + r) * 64 + e] = vh;
+    Wl[((size_t)grp * 128 + r) * 64 + e] = __float2half_rn(v - __half2float(vh));
+    if (live && e <= k && e < F.d) bsum += (double)v * F.mu[(size_t)j * F.d + e];
+  }
+  bias[(size_t)grp * 128 + r] = (float)bsum;
+  if (r < 4) {
+    const int jj = 4 * fg.y + r;
+    const double lc = jj < F.k ? F.logc[jj] : 0.0;
+    chi[(size_t)grp * 4 + r] = jj < F.k ? (float)lc : -INFINITY;
+    clo[(size_t)grp * 4 + r] = jj < F.k ? (float)(lc - (double)(float)lc) : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(kTThreads, 1)
+k_bt_estep(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
+           const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ CUtensorMap tm_wl,
+           const BFit *__restrict__ fits, const BState *__restrict__ state, const EItem *__restrict__ items,
+           int nitems, const float *__restrict__ bias, const float *__restrict__ chi, const float *__restrict__ clo,
+           double *__restrict__ epart, int *err) {
+  using namespace tc;
+  extern __shared__ uint8_t smem_raw[];
+  BTSmem &S = smem_aligned<BTSmem>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; s++) mbar_init(&S.x_full[s], 1), mbar_init(&S.x_empty[s], 1);
+    for (int s = 0; s < kTWS; s++) mbar_init(&S.w_full[s], 1), mbar_init(&S.w_empty[s], 1);
+    for (int s = 0; s < 2; s++) mbar_init(&S.acc_full[s], 1), mbar_init(&S.acc_empty[s], 4);
+    mbar_init(&S.mma_done, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(&S.tmem_base, 256);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = S.tmem_base;
+  // every role walks the same (item, tile, group) sequence
+  if (warp == 0) {
+    if (elect_one()) {
+      uint32_t xi = 0, wi = 0;
+      bool ok = true;
+      for (int ii = blockIdx.x; ii < nitems && ok; ii += gridDim.x) {
+        const EItem it = items[ii];
+        if (!state[it.fit].active) continue;
+        const BFit &F = fits[it.fit];
+        const int ntile = (int)min((int64_t)4, (F.n - it.p0 + kTT - 1) / kTT), G = (F.k + 3) / 4;
+        for (int t = 0; t < ntile && ok; t++) {
+          const int xb = xi & 1;
+          if (!(ok = mbar_wait(&S.x_empty[xb], ((xi >> 1) & 1) ^ 1, err))) break;
+          mbar_expect_tx(&S.x_full[xb], 2 * kTT * 128);
+          const int row = (int)(F.xrow + it.p0 + (int64_t)kTT * t);
+          tma_load_2d(S.xh[xb], &tm_xh, &S.x_full[xb], 0, row);
+          tma_load_2d(S.xl[xb], &tm_xl, &S.x_full[xb], 0, row);
+          xi++;
+          for (int g = 0; g < G; g++) {
+            const int ws = wi % kTWS;
+            if (!(ok = mbar_wait(&S.w_empty[ws], ((wi / kTWS) & 1) ^ 1, err))) break;
+            mbar_expect_tx(&S.w_full[ws], 2 * 128 * 128);
+            tma_load_2d(S.wh[ws], &tm_wh, &S.w_full[ws], 0, (F.wg + g) * 128);
+            tma_load_2d(S.wl[ws], &tm_wl, &S.w_full[ws], 0, (F.wg + g) * 128);
+            wi++;
+          }
+        }
+      }
+      for (int s = 0; s < 2 && xi > (uint32_t)s; s++) {
+        const uint32_t u = xi - 1 - s;
+        mbar_wait_drain(&S.x_full[u & 1], (u >> 1) & 1);
+      }
+      for (int s = 0; s < kTWS && wi > (uint32_t)s; s++) {
+        const uint32_t u = wi - 1 - s;
+        mbar_wait_drain(&S.w_full[u % kTWS], (u / kTWS) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (elect_one()) {
+      uint32_t xi = 0, wi = 0, ai = 0;
+      bool ok = true;
+      for (int ii = blockIdx.x; ii < nitems && ok; ii += gridDim.x) {
+        const EItem it = items[ii];
+        if (!state[it.fit].active) continue;
+        const BFit &F = fits[it.fit];
+        const int ntile = (int)min((int64_t)4, (F.n - it.p0 + kTT - 1) / kTT), G = (F.k + 3) / 4;
+        for (int t = 0; t < ntile && ok; t++) {
+          const int xb = xi & 1;
+          if (!(ok = mbar_wait(&S.x_full[xb], (xi >> 1) & 1, err))) break;
+          tc_fence_after();
+          const uint64_t dxh = sdesc_sw128(smem_u32(S.xh[xb])), dxl = sdesc_sw128(smem_u32(S.xl[xb]));
+          for (int g = 0; g < G && ok; g++) {
+            const int ws = wi % kTWS, ab = ai & 1;
+            if (!(ok = mbar_wait(&S.w_full[ws], (wi / kTWS) & 1, err))) break;
+            if (!(ok = mbar_wait(&S.acc_empty[ab], ((ai >> 1) & 1) ^ 1, err))) break;
+            tc_fence_after();
+            const uint64_t dwh = sdesc_sw128(smem_u32(S.wh[ws])), dwl = sdesc_sw128(smem_u32(S.wl[ws]));
+            const uint32_t dt = tbase + ab * 128;
+            // the small cross products first, x_h W_h last
+#pragma unroll
+            for (int p = 0; p < 3; p++) {
+              const uint64_t da = (p == 1) ? dxl : dxh;
+              const uint64_t db = (p == 0) ? dwl : dwh;
+#pragma unroll
+              for (int kb = 0; kb < 2; kb++)
+                mma_f16(dt, da + 2 * kb, db + 2 * kb, idesc_f16(kTT, kb ? 64 : 128), (p | kb) != 0);
+            }
+            mma_commit(&S.acc_full[ab]);
+            mma_commit(&S.w_empty[ws]);
+            wi++;
+            ai++;
+          }
+          if (!ok) break;
+          mma_commit(&S.x_empty[xb]);
+          xi++;
+        }
+      }
+      mma_commit(&S.mma_done);
+      mbar_wait_drain(&S.mma_done, 0);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 = points of the tile
+    const int quad = warp & 3, row = quad * 32 + lane;
+    const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+    uint32_t ai = 0;
+    int icnt = 0;
+    bool ok = true;
+    for (int ii = blockIdx.x; ii < nitems && ok; ii += gridDim.x) {
+      const EItem it = items[ii];
+      if (!state[it.fit].active) continue;
+      const BFit &F = fits[it.fit];
+      const int64_t n = F.n;
+      const int K = F.k, G = (K + 3) / 4;
+      const int ntile = (int)min((int64_t)4, (n - it.p0 + kTT - 1) / kTT);
+      double lsum = 0.0;
+      for (int t = 0; t < ntile && ok; t++) {
+        const int64_t i = it.p0 + (int64_t)kTT * t + row;
+        const bool valid = i < n;
+        float mx = -INFINITY, se = 0.f;
+        for (int g = 0; g < G; g++) {
+          const int ab = ai & 1;
+          if (!(ok = mbar_wait_warp(&S.acc_full[ab], (ai >> 1) & 1, err))) break;
+          tc_fence_after();
+          uint32_t v[128];
+          tmem_ld64(tbase + lane_addr + ab * 128, *reinterpret_cast<uint32_t(*)[64]>(v));
+          tmem_ld64(tbase + lane_addr + ab * 128 + 64, *reinterpret_cast<uint32_t(*)[64]>(v + 64));
+          tmem_wait_ld();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&S.acc_empty[ab]);
+          ai++;
+          const float *bg = bias + (size_t)(F.wg + g) * 128;
+#pragma unroll
+          for (int q = 0; q < 4; q++) {
+            const int j = 4 * g + q;
+            float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+            for (int u = 0; u < 16; u += 4) {
+              const float4 b0 = __ldg(reinterpret_cast<const float4 *>(bg + 16 * q + u));
+              const float4 b1 = __ldg(reinterpret_cast<const float4 *>(bg + 64 + 16 * q + u));
+              const float a0 = __uint_as_float(v[16 * q + u]) - b0.x, a1 = __uint_as_float(v[16 * q + u + 1]) - b0.y;
+              const float a2 = __uint_as_float(v[16 * q + u + 2]) - b0.z, a3 = __uint_as_float(v[16 * q + u + 3]) - b0.w;
+              const float c0 = __uint_as_float(v[64 + 16 * q + u]) - b1.x;
+              const float c1 = __uint_as_float(v[64 + 16 * q + u + 1]) - b1.y;
+              const float c2 = __uint_as_float(v[64 + 16 * q + u + 2]) - b1.z;
+              const float c3 = __uint_as_float(v[64 + 16 * q + u + 3]) - b1.w;
+              s0 = fmaf(a0, a0, fmaf(a1, a1, fmaf(a2, a2, fmaf(a3, a3, s0))));
+              s1 = fmaf(c0, c0, fmaf(c1, c1, fmaf(c2, c2, fmaf(c3, c3, s1))));
+            }
+            if (j < K) {
+              const float l = (chi[(size_t)(F.wg + g) * 4 + q] - 0.5f * (s0 + s1)) + clo[(size_t)(F.wg + g) * 4 + q];
+              if (valid) F.R[(size_t)j * n + i] = l;
+              blse_push(l, mx, se);
+            }
+          }
+        }
+        if (!ok) break;
+        const float lse = mx + logf(se);
+        if (valid) {
+          lsum += (double)lse;
+          for (int j = 0; j < K; j++) F.R[(size_t)j * n + i] = expf(F.R[(size_t)j * n + i] - lse);
+        }
+      }
+      // the item's LogL partial, summed in a fixed order over the 4 warps
+      const int par = icnt++ & 1;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+      if (lane == 0) S.red[par][warp - 2] = lsum;
+      // the four warps leave together when a wait gave up
+      if (!(ok = bar_and(1, 128, ok))) break;
+      if (threadIdx.x == 64) epart[ii] = ((S.red[par][0] + S.red[par][1]) + S.red[par][2]) + S.red[par][3];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tbase, 256);
+}
 }  // namespace
 }  // namespace fem
 
@@ -941,6 +1198,16 @@ struct fem_em_batch {
   int c_kmax[kClasses] = {};       // largest k of the class's fits
   size_t m_smem[kClasses] = {};     // means kernel dynamic shared memory
   fem_em_batch_tuning tuning{};     // work-item sizes per class
+  // mixed form: tensor-core E-step of the d <= 32 class
+  bool tc = false;
+  int tc_nfits = 0, tc_groups = 0, tc_grid = 0;
+  int64_t tc_rows = 0;
+  int *tfits = nullptr;             // the class's fits
+  int2 *tgroups = nullptr;          // (fit, group) per W group
+  __half *Xh = nullptr, *Xl = nullptr, *Wh = nullptr, *Wl = nullptr;
+  float *tbias = nullptr, *tchi = nullptr, *tclo = nullptr;
+  int *terr = nullptr;              // bounded-wait status of the tensor-core kernel
+  CUtensorMap tm_xh{}, tm_xl{}, tm_wh{}, tm_wl{};
   std::vector<BState> hstate;
   // timing: phase boundaries of the sweeps since the last host sync
   bool timing = false;
@@ -993,6 +1260,16 @@ void free_batch(fem_em_batch *b) {
   dfree(b->mitems);
   dfree(b->citems);
   dfree(b->comps);
+  dfree(b->tfits);
+  dfree(b->tgroups);
+  dfree(b->Xh);
+  dfree(b->Xl);
+  dfree(b->Wh);
+  dfree(b->Wl);
+  dfree(b->tbias);
+  dfree(b->tchi);
+  dfree(b->tclo);
+  dfree(b->terr);
   if (b->hnactive) cudaFreeHost(b->hnactive);
   for (auto &row : b->pev)
     for (auto &e : row)
@@ -1032,6 +1309,15 @@ void collect_timing(fem_em_batch *b, int pending) {
   }
 }
 
+// tensor-core operands of the d <= 32 class from the factorisation just enqueued
+int prep_tc(fem_em_batch *b) {
+  if (!b->tc) return FEM_OK;
+  k_bt_prep<<<b->tc_groups, 128, 0, b->stream>>>(b->fits, b->tgroups, b->Wh, b->Wl, b->tbias, b->tchi, b->tclo);
+  FEM_CUDA(cudaGetLastError());
+  b->launches++;
+  return FEM_OK;
+}
+
 int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
   const BFit *fits = b->fits;
   BState *st = b->state;
@@ -1044,6 +1330,14 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
     }
     const EItem *it0 = b->eitems + b->e_beg[c];
     double *ep = b->epart + b->e_beg[c];
+    if (c == kTClass && b->tc) {
+      k_bt_estep<<<std::min(b->tc_grid, cnt), kTThreads, sizeof(BTSmem) + 1024, b->stream>>>(
+          b->tm_xh, b->tm_xl, b->tm_wh, b->tm_wl, fits, st, it0, cnt, b->tbias, b->tchi, b->tclo, ep, b->terr);
+      FEM_CUDA(cudaGetLastError());
+      b->launches++;
+      mark(b, slot, 1 + c);
+      continue;
+    }
     switch (c) {
       case 0: k_b_estep<4, kBEP><<<cnt, kBEThreads, estep_smem<4>(), b->stream>>>(fits, st, it0, ep); break;
       case 1: k_b_estep<8, kBEP><<<cnt, kBEThreads, estep_smem<8>(), b->stream>>>(fits, st, it0, ep); break;
@@ -1095,6 +1389,7 @@ int launch_sweep(fem_em_batch *b, int it, int svd, int slot) {
   }
   k_b_factor<<<b->ncomps, kBFThreads, 0, b->stream>>>(fits, st, b->comps, b->cpart, b->cfg.reg_coef, 1, svd);
   FEM_CUDA(cudaGetLastError());
+  FEM_TRY(prep_tc(b));
   k_b_sweep_end<<<1, 1024, 0, b->stream>>>(st, b->nfits, it, b->cfg.max_sweeps, b->cfg.eps, b->cfg.abort_thr, svd,
                                            b->trace, b->etrace, b->cap, b->nactive);
   FEM_CUDA(cudaGetLastError());
@@ -1139,8 +1434,8 @@ extern "C" int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t 
     fem_em_config_default(&c);
     c.precision = FEM_PREC_FP32;
   }
-  if (c.precision != FEM_PREC_FP32) {
-    set_error("batched fits run in FP32 on CUDA cores (precision FEM_PREC_FP32)");
+  if (c.precision != FEM_PREC_FP32 && c.precision != FEM_PREC_MIXED) {
+    set_error("batched fits run in FP32 (FEM_PREC_FP32) or with the tensor-core E-step for d > 16 (FEM_PREC_MIXED)");
     return FEM_ERR_UNSUPPORTED;
   }
   if (c.max_sweeps < 1) {
@@ -1204,7 +1499,8 @@ extern "C" int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t 
   std::vector<EItem> ei;
   std::vector<MItem> mi;
   std::vector<CItem> ci;
-  std::vector<int2> comps;
+  std::vector<int2> comps, tgroups;
+  std::vector<int> tfits;
   int64_t mp = 0, cp = 0;
   for (int f = 0; f < nfits; f++) {
     BFit &F = b->hfits[f];
@@ -1222,6 +1518,16 @@ extern "C" int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t 
     F.muT = b->muT + okD[f];
     F.WT = b->WT + okT[f];
     F.logcT = b->logcT + ok_[f];
+    F.xrow = -1;
+    F.wg = 0;
+    if (c.precision == FEM_PREC_MIXED && class_of(d[f]) == kTClass) {
+      F.xrow = b->tc_rows;
+      F.wg = b->tc_groups;
+      b->tc_rows += n[f];
+      for (int g = 0; g < (k[f] + 3) / 4; g++) tgroups.push_back(make_int2(f, g));
+      b->tc_groups += (k[f] + 3) / 4;
+      tfits.push_back(f);
+    }
     for (int j = 0; j < k[f]; j++) comps.push_back(make_int2(f, j));
   }
   for (int c = 0; c < kClasses; c++) {
@@ -1292,6 +1598,31 @@ extern "C" int fem_em_batch_create_tuned(int nfits, const int *d, const int64_t 
       (st = dalloc(&b->trace, (size_t)nfits * b->cap)) || (st = dalloc(&b->etrace, (size_t)nfits * b->cap)) ||
       (st = dalloc(&b->nactive, 1)) || (st = upload_vec(&b->fits, b->hfits)))
     return fail(st);
+  if (!tfits.empty()) {
+    b->tc = true;
+    b->tc_nfits = (int)tfits.size();
+    b->tc_grid = sm_count();
+    if ((st = upload_vec(&b->tfits, tfits)) || (st = upload_vec(&b->tgroups, tgroups)) ||
+        (st = dalloc(&b->Xh, (size_t)b->tc_rows * 64)) || (st = dalloc(&b->Xl, (size_t)b->tc_rows * 64)) ||
+        (st = dalloc(&b->Wh, (size_t)b->tc_groups * 128 * 64)) || (st = dalloc(&b->Wl, (size_t)b->tc_groups * 128 * 64)) ||
+        (st = dalloc(&b->tbias, (size_t)b->tc_groups * 128)) || (st = dalloc(&b->tchi, (size_t)b->tc_groups * 4)) ||
+        (st = dalloc(&b->tclo, (size_t)b->tc_groups * 4)) || (st = dalloc(&b->terr, 1)))
+      return fail(st);
+    if ((st = encode_tmap_2d(&b->tm_xh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, b->Xh, 64, (uint64_t)b->tc_rows, 64, kTT,
+                             CU_TENSOR_MAP_SWIZZLE_128B, 128)) ||
+        (st = encode_tmap_2d(&b->tm_xl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, b->Xl, 64, (uint64_t)b->tc_rows, 64, kTT,
+                             CU_TENSOR_MAP_SWIZZLE_128B, 128)) ||
+        (st = encode_tmap_2d(&b->tm_wh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, b->Wh, 64, (uint64_t)b->tc_groups * 128, 64,
+                             128, CU_TENSOR_MAP_SWIZZLE_128B, 128)) ||
+        (st = encode_tmap_2d(&b->tm_wl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, b->Wl, 64, (uint64_t)b->tc_groups * 128, 64,
+                             128, CU_TENSOR_MAP_SWIZZLE_128B, 128)))
+      return fail(st);
+    if (cudaFuncSetAttribute(k_bt_estep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(BTSmem) + 1024)) != cudaSuccess) {
+      set_error("tensor-core E-step shared-memory limit could not be raised");
+      return fail(FEM_ERR_CUDA);
+    }
+  }
   if (cudaMallocHost((void **)&b->hnactive, sizeof(int)) != cudaSuccess) {
     set_error("pinned allocation failed");
     return fail(FEM_ERR_CUDA);
@@ -1437,10 +1768,18 @@ extern "C" int fem_em_batch_train(fem_em_batch *b, int svd, int *status, int *it
   }
   FEM_CUDA(cudaMemcpyAsync(b->state, b->hstate.data(), b->hstate.size() * sizeof(BState), cudaMemcpyHostToDevice,
                            b->stream));
+  if (b->tc) {
+    // FP16 hi / lo copies of the class's rows (the datasets may have changed since the last train)
+    FEM_CUDA(cudaMemsetAsync(b->terr, 0, sizeof(int), b->stream));
+    k_bt_split<<<dim3(256, b->tc_nfits), 256, 0, b->stream>>>(b->fits, b->tfits, b->Xh, b->Xl);
+    FEM_CUDA(cudaGetLastError());
+    b->launches++;
+  }
   // factorisation of the initial parameters (the fits' psum is not used)
   k_b_factor<<<b->ncomps, kBFThreads, 0, b->stream>>>(b->fits, b->state, b->comps, b->cpart, b->cfg.reg_coef, 0,
                                                       svd);
   FEM_CUDA(cudaGetLastError());
+  FEM_TRY(prep_tc(b));
   k_b_sweep_end<<<1, 1024, 0, b->stream>>>(b->state, b->nfits, 0, b->cfg.max_sweeps, b->cfg.eps, b->cfg.abort_thr,
                                            svd, b->trace, b->etrace, b->cap, b->nactive);
   FEM_CUDA(cudaGetLastError());
@@ -1466,7 +1805,13 @@ extern "C" int fem_em_batch_train(fem_em_batch *b, int svd, int *status, int *it
   }
   FEM_CUDA(cudaMemcpyAsync(b->hstate.data(), b->state, b->hstate.size() * sizeof(BState), cudaMemcpyDeviceToHost,
                            b->stream));
+  int terr = 0;
+  if (b->tc) FEM_CUDA(cudaMemcpyAsync(&terr, b->terr, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   FEM_CUDA(cudaStreamSynchronize(b->stream));
+  if (terr) {
+    set_error("a bounded device wait timed out in the tensor-core E-step");
+    return FEM_ERR_TIMEOUT;
+  }
   int nfail = 0;
   for (int f = 0; f < b->nfits; f++) {
     const BState &s = b->hstate[f];

@@ -165,9 +165,11 @@ int fem_em_timing_covariance(fem_em *h, double *cov_ms);
  * (EM2/EMAlgorithm.cpp:139-191) with the SimpleMatrixEM sweep
  * (EM2/MatrixEM.cpp:275-378), on its own data, with its own convergence test
  * and failure status.  Every kernel of a sweep covers all fits still
- * sweeping.  FP32 on CUDA cores with FP64 partial sums, factorisation and
- * LogL: cfg->precision must be FEM_PREC_FP32 (cfg NULL: the reference
- * defaults with FP32).  Per fit d <= 32, k <= 64, n < 2^31 (larger shapes:
+ * sweeping.  FEM_PREC_FP32: FP32 on CUDA cores with FP64 partial sums,
+ * factorisation and LogL (cfg NULL: the reference defaults with FP32).
+ * FEM_PREC_MIXED: the same, except that the E-step of the fits with
+ * 16 < d <= 32 runs on the tensor cores (FP16 x 3 split products, FP32
+ * accumulation).  Per fit d <= 32, k <= 64, n < 2^31 (larger shapes:
  * FEM_ERR_UNSUPPORTED). */
 typedef struct fem_em_batch fem_em_batch;
 

@@ -25,9 +25,9 @@ def fits(shapes=SHAPES, seed_shift=0):
     return out
 
 
-def train_batch(data, sweeps, eps=0.0, abort_thr=1e12, reg=0.0, svd=False, tuning="table"):
+def train_batch(data, sweeps, eps=0.0, abort_thr=1e12, reg=0.0, svd=False, tuning="table", precision="fp32"):
     shapes = [(X.shape[1], X.shape[0], len(init[0])) for X, init in data]
-    with CudaBatchEM(shapes, tuning=tuning) as B:
+    with CudaBatchEM(shapes, tuning=tuning, precision=precision) as B:
         B.SetParameters(sweeps, eps, abort_thr, reg)
         st, it, ll = B.Train([X for X, _ in data], [GaussianMixture(*init) for _, init in data], svd=svd)
         traces = [B.Trace(i) for i in range(len(data))]
@@ -42,13 +42,17 @@ TUNINGS = {"default": None, "small": {"means_chunk": [512] * 4, "cov_chunk": [10
            "large": {"means_chunk": [8192] * 4, "cov_chunk": [8192] * 4}, "table": "table"}
 
 
-@pytest.mark.parametrize("tuning", list(TUNINGS))
+@pytest.mark.parametrize("tuning", list(TUNINGS) + ["mixed"])
 def test_batch_matches_oracle(gpu_lib, oracle, tuning):
     """10 sweeps of every fit: |dlogL/N| <= 1e-5 per sweep against the FP64
     oracle (FP32 per-point terms, FP64 sums), same IterCounter, means and
-    weights close -- whatever the work-item sizes."""
+    weights close -- whatever the work-item sizes, and with the tensor-core
+    E-step of the d > 16 fits (mixed)."""
     data = fits()
-    got = train_batch(data, 10, tuning=TUNINGS[tuning])
+    if tuning == "mixed":
+        got = train_batch(data, 10, precision="mixed")
+    else:
+        got = train_batch(data, 10, tuning=TUNINGS[tuning])
     for i, (X, init) in enumerate(data):
         ref = oracle.em_train(X, *init, 10, eps=0.0, abort_thr=1e12)
         assert ref["status"] == 0
@@ -171,3 +175,25 @@ def test_batch_edge_shapes(gpu_lib, oracle):
         assert ref["status"] == 0 and got["status"][i] == 0 and got["iters"][i] == ref["iter_counter"]
         err = np.max(np.abs(got["traces"][i][0] - ref["logl"])) / len(X)
         assert err <= 1e-5, (shapes[i], err)
+
+
+def test_batch_mixed_mixes_classes_and_ragged_tiles(gpu_lib, oracle):
+    """mixed: fits of every class in one batch, the d > 16 ones with n not a
+    multiple of the 128-point tile and k not a multiple of 4 (padding
+    components), against the oracle and against the FP32 batch"""
+    shapes = [(20, 1000 + 37, 5, 301), (32, 777, 9, 302), (8, 3000, 6, 303), (17, 4321, 13, 304),
+              (4, 2000, 3, 305), (30, 129, 2, 306)]
+    data = fits(shapes)
+    got = train_batch(data, 6, precision="mixed")
+    f32 = train_batch(data, 6)
+    for i, (X, init) in enumerate(data):
+        ref = oracle.em_train(X, *init, 6, eps=0.0, abort_thr=1e12)
+        if ref["status"] != 0:
+            continue
+        ll, _ = got["traces"][i]
+        err = np.max(np.abs(ll - ref["logl"])) / len(X)
+        print(i, X.shape, "mixed |dlogL/N| =", err)
+        assert err <= 1e-5, (i, err)
+        if X.shape[1] <= 16:
+            # the same CUDA-core kernels as the FP32 batch
+            np.testing.assert_array_equal(ll, f32["traces"][i][0])
