@@ -25,8 +25,10 @@
 // Kernels:
 //  1. k_wide_prep: W_j = L_j^-1 as FP16 hi + lo, rows permuted so that each
 //     64-dim input chunk's nonzero part of the triangle is a row prefix, with
-//     a power-of-two scale per row (no FP16 overflow or underflow whatever the
-//     covariance scale); centres m_j, offsets b_j, log coefficients.
+//     a power-of-two scale per component (its largest entry in [2^13, 2^14):
+//     no FP16 overflow whatever the covariance scale, and the rows' largest
+//     entries differ by sqrt(cond), so every row stays in FP16's normal range
+//     up to condition ~1e9); centres m_j, offsets b_j, log coefficients.
 //  2. k_wide_estep (EM2/MatrixEM.cpp:39-51,69-81): one CTA per SM walks (tile
 //     of 128 points, component j) units.  The tile's FP32 rows live in tensor
 //     memory; producer warps form a = x - m_j, split it into FP16 hi / lo
@@ -116,7 +118,7 @@ struct WideEmPlan {
   int egrid = 0, cgrid = 0, nslot = 0;
   __half *Wh = nullptr, *Wl = nullptr;   // K x Dp x Dp, permuted rows
   float *cen = nullptr;           // K x Dp centres m = fp16(mu)
-  float *wsc = nullptr;           // K x Dp row scales (powers of two), permuted
+  float *wsc = nullptr;           // K component scales (powers of two)
   float *wb = nullptr;            // K x Dp offsets b = W (mu - m), permuted
   float *chi = nullptr, *clo = nullptr;  // log coefficient as float hi + lo
   double *Lw = nullptr;           // K x d x d Cholesky factors of the E-step
@@ -139,10 +141,17 @@ __device__ __forceinline__ void w_store_post(__half *Rh, __half *Rl, size_t o, f
 
 __device__ __forceinline__ uint32_t h2_bits(__half2 v) { return *reinterpret_cast<uint32_t *>(&v); }
 
+// FP32 -> FP16, round to nearest, values beyond the FP16 range to +-65504
+__device__ __forceinline__ __half half_satfinite(float x) {
+  unsigned short u;
+  asm("cvt.rn.satfinite.f16.f32 %0, %1;" : "=h"(u) : "f"(x));
+  return __ushort_as_half(u);
+}
+
 // ============================================================== prepare
-// Row k of W_j (output dim k) goes to row p = Dp - 1 - k, scaled by 2^-e_k
-// so that its largest entry lies in [2^13, 2^14) (wsc = 2^e_k undoes it on
-// the accumulator); padded rows and columns are zero.
+// Row k of W_j (output dim k) goes to row p = Dp - 1 - k, scaled by 2^-e so
+// that the component's largest entry lies in [2^13, 2^14) (wsc = 2^e undoes
+// it on the accumulator); padded rows and columns are zero.
 __global__ void __launch_bounds__(256)
 k_wide_prep(const double *__restrict__ linv, const double *__restrict__ chol, const double *__restrict__ mu,
             const double *__restrict__ logc, int d, int Dp, __half *__restrict__ Wh, __half *__restrict__ Wl,
@@ -152,7 +161,8 @@ k_wide_prep(const double *__restrict__ linv, const double *__restrict__ chol, co
   const double *Wi = linv + (size_t)j * d * d;
   const double *A = chol + (size_t)j * d * d;
   __shared__ double dm[kWMax];      // mu - m
-  __shared__ double rsc[kWMax];     // 2^-e per output dim
+  __shared__ double rmax[256];
+  __shared__ double s_rsc;          // 2^-e
   for (int e = threadIdx.x; e < Dp; e += blockDim.x) {
     double m = 0.0, r = 0.0;
     if (e < d) {
@@ -163,20 +173,24 @@ k_wide_prep(const double *__restrict__ linv, const double *__restrict__ chol, co
     cen[(size_t)j * Dp + e] = (float)m;
     dm[e] = r;
   }
-  for (int k = threadIdx.x; k < Dp; k += blockDim.x) {
-    double mx = 0.0;
-    if (k < d)
-      for (int c = 0; c <= k; c++) mx = fmax(mx, fabs(Wi[(size_t)k * d + c]));
+  double mx = 0.0;
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) mx = fmax(mx, fabs(Wi[e]));
+  rmax[threadIdx.x] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int t = 0; t < (int)blockDim.x; t++) m = fmax(m, rmax[t]);
     int ex = 0;
-    if (mx > 0.0) frexp(mx, &ex);   // mx = f 2^ex, f in [0.5, 1)
-    const int sh = ex - 14;         // mx 2^-sh in [2^13, 2^14)
-    rsc[k] = ldexp(1.0, -sh);
-    wsc[(size_t)j * Dp + (Dp - 1 - k)] = (float)ldexp(1.0, sh);
+    if (m > 0.0) frexp(m, &ex);     // m = f 2^ex, f in [0.5, 1)
+    const int sh = ex - 14;         // m 2^-sh in [2^13, 2^14)
+    s_rsc = ldexp(1.0, -sh);
+    wsc[j] = (float)ldexp(1.0, sh);
   }
   __syncthreads();
+  const double rsc = s_rsc;
   for (int e = threadIdx.x; e < Dp * Dp; e += blockDim.x) {
     const int k = e / Dp, c = e - k * Dp;
-    const double w = (k < d && c <= k) ? Wi[(size_t)k * d + c] * rsc[k] : 0.0;
+    const double w = (k < d && c <= k) ? Wi[(size_t)k * d + c] * rsc : 0.0;
     const __half h = __double2half(w);
     const size_t o = ((size_t)j * Dp + (Dp - 1 - k)) * Dp + c;
     Wh[o] = h;
@@ -400,7 +414,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
         if (ok) {
           tc_fence_after();
           const float *bj = wb + (size_t)j * Dp;
-          const float *sj = wsc + (size_t)j * Dp;
+          const float sc = wsc[j];
           __half *yj = Y + (size_t)j * Dp * np + (pi >= 0 ? pi : 0);
           for (int q = eg; q < nc; q += 2) {
             uint32_t v[64];
@@ -416,18 +430,16 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
             for (int u = 0; u < 16; u++) {
               const int p0 = 64 * q + 4 * u;
               const float4 b = __ldg(reinterpret_cast<const float4 *>(bj + p0));
-              const float4 sc = __ldg(reinterpret_cast<const float4 *>(sj + p0));
-              const float y[4] = {fmaf(__uint_as_float(v[4 * u]), sc.x, -b.x),
-                                  fmaf(__uint_as_float(v[4 * u + 1]), sc.y, -b.y),
-                                  fmaf(__uint_as_float(v[4 * u + 2]), sc.z, -b.z),
-                                  fmaf(__uint_as_float(v[4 * u + 3]), sc.w, -b.w)};
+              const float y[4] = {fmaf(__uint_as_float(v[4 * u]), sc, -b.x),
+                                  fmaf(__uint_as_float(v[4 * u + 1]), sc, -b.y),
+                                  fmaf(__uint_as_float(v[4 * u + 2]), sc, -b.z),
+                                  fmaf(__uint_as_float(v[4 * u + 3]), sc, -b.w)};
 #pragma unroll
               for (int e = 0; e < 4; e++) {
                 s4[e] = fmaf(y[e], y[e], s4[e]);
                 // output dim k = Dp - 1 - p; |y| beyond the FP16 range only occurs
                 // where the posterior is 0 (the M-step multiplies it by sqrt r = 0)
-                if (pi >= 0)
-                  yj[(size_t)(Dp - 1 - (p0 + e)) * np] = __float2half_rn(fminf(fmaxf(y[e], -65504.f), 65504.f));
+                if (pi >= 0) yj[(size_t)(Dp - 1 - (p0 + e)) * np] = half_satfinite(y[e]);
               }
             }
           }
@@ -875,7 +887,7 @@ int em_wide_create(fem_em *h) {
   FEM_TRY(dalloc(&p->Wh, kdp * Dp));
   FEM_TRY(dalloc(&p->Wl, kdp * Dp));
   FEM_TRY(dalloc(&p->cen, kdp));
-  FEM_TRY(dalloc(&p->wsc, kdp));
+  FEM_TRY(dalloc(&p->wsc, (size_t)K));
   FEM_TRY(dalloc(&p->wb, kdp));
   FEM_TRY(dalloc(&p->chi, K));
   FEM_TRY(dalloc(&p->clo, K));
