@@ -41,7 +41,7 @@
 //     the accumulator back 64 columns at a time (it zeroes what it read).
 //  3. k_wide_cov: z = fp16(sqrt r) * y for 64-point blocks of one component,
 //     M = z z^T (two M = 128 products: dims 0..127 x 0..127 and 128..255 x
-//     0..255) in FP32 TMEM windows of 4096 points, flushed to FP64; producers
+//     0..255) in FP32 TMEM windows of 16384 points, flushed to FP64; producers
 //     also sum r, r y and the diagonal z_a^2 in FP32 (round to nearest).  The
 //     tensor core's FP32 accumulation drops an addend's bits below the
 //     accumulator's ulp (toward zero): harmless for the off-diagonal sums,
@@ -82,8 +82,13 @@ constexpr int kWEThreads = 448;
 constexpr int kWEpi0 = 6;           // first epilogue warp
 constexpr int kVBlk = 64;           // covariance kernel: points per block
 constexpr int kVS = 5;              // covariance input ring
-constexpr int kVWin = 64;           // blocks per FP32 accumulation window (4096 points)
-constexpr int kWCThreads = 320;     // warp 0 TMA, 1 MMA, 2..5 producers, 6..9 flush
+// blocks per FP32 accumulation window (16384 points): the window sums only the
+// off-diagonal terms (increments of either sign; the diagonal is summed by the
+// producers), and each flush stalls the MMAs while 393 KB of FP64 partials are
+// read and written
+constexpr int kVWin = 256;
+constexpr int kWCThreads = 448;     // warp 0 TMA, 1 MMA, 2..9 producers (one row each), 10..13 flush
+constexpr int kWCFlush0 = 10;       // first flush warp
 // per (CTA, component) sums: r y (kWMax), z_a^2 (kWMax), r (64 partials)
 constexpr int kSPart = 2 * kWMax + kVBlk;
 constexpr int kWMaxGrid = 256;      // covariance CTAs at most (a component may meet all of them)
@@ -510,7 +515,7 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       reinterpret_cast<uint4 *>(S.y[s] + Dp * kVBlk)[r] = make_uint4(0, 0, 0, 0);
     }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kVS; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.z_full[s], 4), mbar_init(&S.in_empty[s], 1);
+    for (int s = 0; s < kVS; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.z_full[s], 8), mbar_init(&S.in_empty[s], 1);
     mbar_init(&S.acc_full, 1);
     mbar_init(&S.acc_empty, 4);
     mbar_init(&S.mma_done, 1);
@@ -579,15 +584,15 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       mma_commit(&S.mma_done);
       mbar_wait_drain(&S.mma_done, 0);
     }
-  } else if (warp < 6) {
+  } else if (warp < kWCFlush0) {
     // ------------------------------------------------ producers: z = fp16(sqrt r) y in place
-    const int p = threadIdx.x - 64;   // rows p and p + 128
+    const int p = threadIdx.x - 64;   // row p
     uint32_t i = 0;
     bool ok = true;
     // sum r, sum r y and sum z^2 (the diagonal: its increments are all positive,
-    // which the tensor core's truncating accumulation would bias low) of rows
-    // p and p + 128 over the segment
-    double s0 = 0.0, s1[2] = {0.0, 0.0}, s2[2] = {0.0, 0.0};
+    // which the tensor core's truncating accumulation would bias low) of row p
+    // over the segment
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
     for (int64_t f = f0; f < f1 && ok; f++, i++) {
       const int s = i % kVS;
       ok = mbar_wait_warp(&S.in_full[s], (i / kVS) & 1, err);
@@ -597,10 +602,9 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
         s0 += (double)r;
       }
       // every producer leaves together when one of them gave up
-      if (!(ok = bar_and(1, 128, ok))) break;
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int rw = p + 128 * h;
+      if (!(ok = bar_and(1, 256, ok))) break;
+      {
+        const int rw = p;
         if (rw < Dp) {
           uint8_t *rp = reinterpret_cast<uint8_t *>(S.y[s]) + rw * 128;
           float acc = 0.f, sq = 0.f;
@@ -623,8 +627,8 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
             }
             *reinterpret_cast<uint4 *>(rp + q * 16) = v;
           }
-          s1[h] += (double)acc;
-          s2[h] += (double)sq;
+          s1 += (double)acc;
+          s2 += (double)sq;
         }
       }
       fence_async_shared();
@@ -632,12 +636,10 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       if (lane == 0) mbar_arrive(&S.z_full[s]);
       if (f == f1 - 1 || (f % nbk) == nbk - 1) {
         double *sp = spart + ((size_t)blockIdx.x * nslot + ((int)(f / nbk) - j0)) * kSPart;
-        sp[p] = s1[0];
-        sp[p + 128] = s1[1];
-        sp[kWMax + p] = s2[0];
-        sp[kWMax + p + 128] = s2[1];
+        sp[p] = s1;
+        sp[kWMax + p] = s2;
         if (p < kVBlk) sp[2 * kWMax + p] = s0;
-        s0 = 0.0, s1[0] = s1[1] = 0.0, s2[0] = s2[1] = 0.0;
+        s0 = 0.0, s1 = 0.0, s2 = 0.0;
       }
     }
   } else {
