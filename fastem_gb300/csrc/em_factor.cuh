@@ -92,6 +92,168 @@ __device__ inline void block_lower_inverse(const double *A, int d, double *Wi) {
   __syncthreads();
 }
 
+// ------------------------------------------------------------------------
+// Blocked forms of block_cholesky and block_lower_inverse for one CTA of
+// kFactorThreads threads (d <= kFactorMaxD).  Each matrix element goes through
+// the same FP64 operations in the same order as in the unblocked functions (a
+// running a - x y per update, k ascending), so the factors are bit-identical;
+// the blocking only changes where the operands live.  With one CTA per
+// component the unblocked loops wait on L2 for every element update; here the
+// panel being factored and the row block being inverted sit in shared memory,
+// the trailing updates are 4 x 4 register tiles, and the FP64 pipe is the
+// limit (d^3 / 6 fused multiply-adds each for the factor and the inverse).
+constexpr int kFactorThreads = 256;
+constexpr int kPanel = 32;                // columns per Cholesky panel, rows per inverse block
+constexpr int kPanelLd = kPanel + 1;      // panel row stride (doubles)
+constexpr int kFactorBlockedD = 128;      // smallest d that the blocked forms are used for
+
+// dynamic shared memory of the two functions (the panel, then the row block)
+__host__ __device__ constexpr size_t factor_smem_bytes(int d) {
+  return (size_t)d * kPanelLd * sizeof(double);
+}
+
+// block_cholesky with panels of kPanel columns: the panel (rows k0 .. d-1)
+// is factored in shared memory (thread i owns row k0 + i), written back, and
+// its update of the trailing lower triangle applied as 4 x 4 tiles.  The
+// upper triangle of A keeps the symmetric copy of S, as in block_cholesky.
+// P: factor_smem_bytes(d) of shared memory.  Returns true on success, the
+// same in every thread.
+__device__ inline bool block_cholesky_panels(const double *S, int d, double *A, double *P) {
+  __shared__ double s_diag[kPanel];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < d * d; e += nt) {
+    const int r = e / d, c = e - r * d;
+    A[e] = (c <= r) ? S[e] : S[(size_t)c * d + r];
+  }
+  __syncthreads();
+  bool ok = true;
+  for (int k0 = 0; k0 < d; k0 += kPanel) {
+    const int w = min(kPanel, d - k0), m = d - k0;
+    for (int e = tid; e < m * w; e += nt) {
+      const int i = e / w, q = e - i * w;
+      P[i * kPanelLd + q] = A[(size_t)(k0 + i) * d + k0 + q];
+    }
+    __syncthreads();
+    const int i = tid;                    // panel row owned by this thread
+    for (int q = 0; q < w; q++) {
+      const double x = P[q * kPanelLd + q];   // the same value in every thread
+      if (!(x > 0.0)) {
+        ok = false;
+        break;
+      }
+      const double l = sqrt(x);
+      if (i == q) s_diag[q] = l;
+      if (i > q && i < m) P[i * kPanelLd + q] = P[i * kPanelLd + q] / l;
+      __syncthreads();
+      if (i > q && i < m) {
+        const double lik = P[i * kPanelLd + q];
+        const int ce = min(i, w - 1);
+        for (int c = q + 1; c <= ce; c++)
+          P[i * kPanelLd + c] = fma(-lik, P[c * kPanelLd + q], P[i * kPanelLd + c]);
+      }
+      __syncthreads();
+    }
+    if (!ok) break;
+    for (int e = tid; e < m * w; e += nt) {
+      const int r = e / w, q = e - r * w;
+      if (q <= r) A[(size_t)(k0 + r) * d + k0 + q] = (q == r) ? s_diag[q] : P[r * kPanelLd + q];
+    }
+    // trailing update: A[r][c] -= sum_q L[r][q] L[c][q], w <= c <= r < m
+    // (panel-relative), over 4 x 4 tiles of the lower triangle
+    const int n2 = m - w;
+    if (n2 > 0) {
+      const int T = (n2 + 3) >> 2;
+      const int ntile = T * (T + 1) / 2;
+      for (int t = tid; t < ntile; t += nt) {
+        int ti = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+        while ((ti + 1) * (ti + 2) / 2 <= t) ti++;
+        while (ti * (ti + 1) / 2 > t) ti--;
+        const int tc = t - ti * (ti + 1) / 2;
+        const int rb = w + 4 * ti, cb = w + 4 * tc;
+        double acc[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int v = 0; v < 4; v++) {
+            const int r = rb + u, c = cb + v;
+            acc[u][v] = (r < m && c <= r) ? A[(size_t)(k0 + r) * d + k0 + c] : 0.0;
+          }
+        for (int q = 0; q < w; q++) {
+          double a[4], b[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            a[u] = (rb + u < m) ? P[(rb + u) * kPanelLd + q] : 0.0;
+            b[u] = (cb + u < m) ? P[(cb + u) * kPanelLd + q] : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int v = 0; v < 4; v++) acc[u][v] = fma(-a[u], b[v], acc[u][v]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int v = 0; v < 4; v++) {
+            const int r = rb + u, c = cb + v;
+            if (r < m && c <= r) A[(size_t)(k0 + r) * d + k0 + c] = acc[u][v];
+          }
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  return ok;
+}
+
+// block_lower_inverse by blocks of kPanel rows, thread c owning column c of
+// W = L^-1 (d <= blockDim.x): the block's rows of L are staged in shared
+// memory (Lb); the terms of the rows above the block (m < r0) run as a
+// register-blocked product over the thread's own column of W, then the
+// block's triangle is solved row by row with that column's new entries in
+// registers.  Terms with m < c multiply an exact zero of W and leave the
+// running sum unchanged, so the loops need no per-column bounds.
+__device__ inline void block_lower_inverse_rows(const double *A, int d, double *Wi, double *Lb) {
+  __shared__ double s_rd[kFactorMaxD];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int r = tid; r < d; r += nt) s_rd[r] = 1.0 / A[(size_t)r * d + r];
+  const int c = tid;
+  for (int r0 = 0; r0 < d; r0 += kPanel) {
+    const int rb = min(kPanel, d - r0), mw = r0 + rb;   // block rows, columns of L used
+    __syncthreads();                                    // Lb free (and s_rd formed)
+    for (int e = tid; e < kPanel * mw; e += nt) {
+      const int rr = e / mw, m = e - rr * mw;
+      Lb[rr * mw + m] = rr < rb ? A[(size_t)(r0 + rr) * d + m] : 0.0;
+    }
+    __syncthreads();
+    if (c >= d) continue;
+    if (c >= mw) {                                      // above the diagonal
+      for (int rr = 0; rr < rb; rr++) Wi[(size_t)(r0 + rr) * d + c] = 0.0;
+      continue;
+    }
+    double acc[kPanel];
+#pragma unroll
+    for (int rr = 0; rr < kPanel; rr++) acc[rr] = 0.0;
+    for (int m = c; m < r0; m++) {                      // rows above the block
+      const double wm = Wi[(size_t)m * d + c];
+#pragma unroll
+      for (int rr = 0; rr < kPanel; rr++) acc[rr] = fma(-Lb[rr * mw + m], wm, acc[rr]);
+    }
+    double wb[kPanel];
+#pragma unroll
+    for (int rr = 0; rr < kPanel; rr++) {               // the block's triangle
+      if (rr < rb) {
+        const int r = r0 + rr;
+        double s = c < r0 ? acc[rr] : (r == c ? 1.0 : 0.0);
+#pragma unroll
+        for (int mm = 0; mm < rr; mm++) s = fma(-Lb[rr * mw + r0 + mm], wb[mm], s);
+        wb[rr] = r < c ? 0.0 : s * s_rd[r];
+        Wi[(size_t)r * d + c] = wb[rr];
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // log det = 2 sum log L_ii (L in the lower triangle of A): the logarithms in
 // parallel, summed in index order by one thread; the value in every thread.
 // d <= kFactorMaxD.
