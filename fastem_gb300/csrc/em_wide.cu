@@ -98,6 +98,9 @@ struct __align__(1024) WESmem {
   __half al[kWAS][kWTile * 64];   // FP16 lo
   __half wh[kWWS][kWMax * 64];    // W chunk: rows = permuted output dims, 64 input dims
   __half wl[kWWS][kWMax * 64];
+  // y of one 64-column quarter per epilogue group, rows = output dims (64),
+  // 128 points each: the source of the group's TMA store into Y
+  __half ys[2][64 * kWTile];
   uint64_t a_full[kWAS], a_empty[kWAS], w_full[kWWS], w_empty[kWWS];
   uint64_t acc_full, acc_empty[4], mma_done;
   uint32_t tmem_base;
@@ -117,6 +120,7 @@ static_assert(sizeof(WCSmem) + 1024 <= 232448, "wide covariance shared memory");
 
 struct WideEmPlan {
   CUtensorMap tm_wh, tm_wl, tm_y, tm_rh, tm_rl;
+  CUtensorMap tm_ys;              // Y as stored by the E-step: 128 points x 64 dims
   int Dp = 0;                     // d rounded up to a multiple of 64
   int64_t np = 0;                 // posterior / y row pitch (multiple of 64)
   int64_t nbk = 0;                // 64-point blocks
@@ -220,7 +224,7 @@ k_wide_prep(const double *__restrict__ linv, const double *__restrict__ chol, co
 // ============================================================== E-step
 __global__ void __launch_bounds__(kWEThreads, 1)
 k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ CUtensorMap tm_wl,
-             const float *__restrict__ X, const float *__restrict__ cen, const float *__restrict__ wsc,
+             const __grid_constant__ CUtensorMap tm_ys, const float *__restrict__ X, const float *__restrict__ cen, const float *__restrict__ wsc,
              const float *__restrict__ wb, const float *__restrict__ chi, const float *__restrict__ clo,
              const double *__restrict__ c64, float *__restrict__ lsc, __half *__restrict__ Rh,
              __half *__restrict__ Rl, __half *__restrict__ Y, int64_t np, double *__restrict__ part, int64_t n,
@@ -387,6 +391,13 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
     // 0 also keeps the log-sum-exp and writes the posteriors
     const int quad = warp & 3, row = quad * 32 + lane, eg = (warp - kWEpi0) >> 2;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+    // y leaves through the group's staging tile and one TMA store per quarter
+    // (64 dims x 128 points, whole 256-byte rows): written by the threads
+    // directly, y would go out as 64-byte pieces of 64 rows 2 np bytes apart,
+    // and those scattered stores took half of the kernel's time
+    const int gbar = 3 + eg;                      // the group's named barrier
+    const bool issuer = warp == kWEpi0 + 4 * eg && lane == 0;
+    __half *ys = S.ys[eg];
     // l_ij scratch of this CTA: [tile parity][component][128 points]
     float *scr = lsc + (size_t)blockIdx.x * 2 * K * kWTile + row;
     // the accumulator starts at zero and is zeroed as it is read: every MMA accumulates
@@ -415,12 +426,13 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
         float lp = 0.f;
         if (eg == 0 && have_prev && prev_i >= 0) lp = scr[(size_t)(prev_par * K + j) * kWTile];
         ok = mbar_wait_warp(&S.acc_full, ui & 1, err);
+        // the group's warps take the same branch (its named barrier is inside)
+        ok = bar_and(gbar, 128, ok);
         float s4[4] = {0.f, 0.f, 0.f, 0.f};
         if (ok) {
           tc_fence_after();
           const float *bj = wb + (size_t)j * Dp;
           const float sc = wsc[j];
-          __half *yj = Y + (size_t)j * Dp * np + (pi >= 0 ? pi : 0);
           for (int q = eg; q < nc; q += 2) {
             uint32_t v[64];
             tmem_ld64(tbase + lane_addr + 64 * q, v);
@@ -431,6 +443,9 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&S.acc_empty[q]);
+            // the staging tile is free once the group's previous store has read it
+            if (issuer) bulk_wait_read();
+            named_bar_sync(gbar, 128);
 #pragma unroll
             for (int u = 0; u < 16; u++) {
               const int p0 = 64 * q + 4 * u;
@@ -442,10 +457,18 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
 #pragma unroll
               for (int e = 0; e < 4; e++) {
                 s4[e] = fmaf(y[e], y[e], s4[e]);
-                // output dim k = Dp - 1 - p; |y| beyond the FP16 range only occurs
-                // where the posterior is 0 (the M-step multiplies it by sqrt r = 0)
-                if (pi >= 0) yj[(size_t)(Dp - 1 - (p0 + e)) * np] = half_satfinite(y[e]);
+                // output dim k = Dp - 1 - p, staging row k - (Dp - 64 - 64 q); |y|
+                // beyond the FP16 range only occurs where the posterior is 0 (the
+                // M-step multiplies it by sqrt r = 0)
+                ys[(63 - 4 * u - e) * kWTile + row] = half_satfinite(y[e]);
               }
+            }
+            fence_async_shared();
+            named_bar_sync(gbar, 128);
+            // points past n are not written (the tensor map's extent)
+            if (issuer) {
+              tma_store_2d(&tm_ys, ys, (int)(tile * kWTile), j * Dp + Dp - 64 - 64 * q);
+              bulk_commit();
             }
           }
         }
@@ -485,6 +508,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       asm volatile("bar.sync 1, 128;" ::: "memory");
       if (threadIdx.x == kWEpi0 * 32) part[blockIdx.x] = ((S.red[0] + S.red[1]) + S.red[2]) + S.red[3];
     }
+    if (issuer) bulk_wait_all();
   }
   tc_fence_before();
   __syncthreads();
@@ -918,6 +942,8 @@ int em_wide_create(fem_em *h) {
   // points past n read as zero (posterior 0, y 0)
   FEM_TRY(encode_tmap_2d(&p->tm_y, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Y, (uint64_t)n, (uint64_t)K * Dp, kVBlk,
                          64, CU_TENSOR_MAP_SWIZZLE_128B, (uint64_t)p->np * 2));
+  FEM_TRY(encode_tmap_2d(&p->tm_ys, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Y, (uint64_t)n, (uint64_t)K * Dp, kWTile,
+                         64, CU_TENSOR_MAP_SWIZZLE_NONE, (uint64_t)p->np * 2));
   FEM_TRY(encode_tmap_2d(&p->tm_rh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rh, (uint64_t)n, (uint64_t)K, kVBlk, 1,
                          CU_TENSOR_MAP_SWIZZLE_NONE, (uint64_t)p->np * 2));
   FEM_TRY(encode_tmap_2d(&p->tm_rl, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, p->Rl, (uint64_t)n, (uint64_t)K, kVBlk, 1,
@@ -986,7 +1012,7 @@ int em_wide_prepare(fem_em *h) {
 int em_wide_estep(fem_em *h) {
   WideEmPlan *p = h->wide;
   k_wide_estep<<<p->egrid, kWEThreads, wesmem_bytes(), h->stream>>>(
-      p->tm_wh, p->tm_wl, h->X, p->cen, p->wsc, p->wb, p->chi, p->clo, h->logc, p->lsc, p->Rh, p->Rl, p->Y, p->np,
+      p->tm_wh, p->tm_wl, p->tm_ys, h->X, p->cen, p->wsc, p->wb, p->chi, p->clo, h->logc, p->lsc, p->Rh, p->Rl, p->Y, p->np,
       p->epart, h->n, h->d, p->Dp, h->k, p->err);
   FEM_CUDA(cudaGetLastError());
   k_wide_reduce<<<1, 32, 0, h->stream>>>(p->epart, p->egrid, h->dstat, p->err);
