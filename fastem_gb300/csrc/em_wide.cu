@@ -74,6 +74,11 @@ constexpr int kWMax = 256;          // widest padded dimension
 constexpr int kWTile = 128;         // E-step points per tile (MMA M)
 constexpr int kWAS = 2;             // centred-x operand ring (64-dim chunks)
 constexpr int kWWS = 2;             // W operand ring (64-dim chunks)
+// W stage 0 holds at most kWS0 rows: with four chunks per unit it receives
+// chunks 3 and 1 (64 and 192 rows), stage 1 chunks 2 and 0 (128 and 256);
+// with three or two chunks every chunk has at most 192 rows
+constexpr int kWS0 = 192;
+constexpr int kWCS = 4;             // ring of per-component vectors (m, b)
 constexpr uint32_t kWXCol = 256;    // TMEM column of the tile's FP32 rows
 // warp 0 TMA, 1 MMA, 2..5 producers, 6..13 epilogue (two groups of 4 warps that
 // read alternate 64-column quarters).  14 warps are allocated as 16, which
@@ -96,12 +101,15 @@ constexpr int kWMaxGrid = 256;      // covariance CTAs at most (a component may 
 struct __align__(1024) WESmem {
   __half ah[kWAS][kWTile * 64];   // a = x - m, FP16 hi: rows = points, 64 dims, SW128
   __half al[kWAS][kWTile * 64];   // FP16 lo
-  __half wh[kWWS][kWMax * 64];    // W chunk: rows = permuted output dims, 64 input dims
-  __half wl[kWWS][kWMax * 64];
+  __half wh[(kWS0 + kWMax) * 64]; // W chunk stages: rows = permuted output dims, 64 input dims
+  __half wl[(kWS0 + kWMax) * 64];
   // y of one 64-column quarter per epilogue group, rows = output dims (64),
   // 128 points each: the source of the group's TMA store into Y
   __half ys[2][64 * kWTile];
-  uint64_t a_full[kWAS], a_empty[kWAS], w_full[kWWS], w_empty[kWWS];
+  // centre m_j and offset b_j of the units in flight, fetched by the TMA warp
+  // (global loads of them would put an L2 round trip into every chunk)
+  float cvm[kWCS][kWMax], cvb[kWCS][kWMax];
+  uint64_t a_full[kWAS], a_empty[kWAS], w_full[kWWS], w_empty[kWWS], cv_full[kWCS], cv_empty[kWCS];
   uint64_t acc_full, acc_empty[4], mma_done;
   uint32_t tmem_base;
   float ssum[2][kWTile];          // second epilogue group's partial sums of y^2 (by unit parity)
@@ -222,6 +230,8 @@ k_wide_prep(const double *__restrict__ linv, const double *__restrict__ chol, co
 }
 
 // ============================================================== E-step
+__device__ __forceinline__ __half *w_stage(__half *w, int s) { return w + (s ? kWS0 * 64 : 0); }
+
 __global__ void __launch_bounds__(kWEThreads, 1)
 k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ CUtensorMap tm_wl,
              const __grid_constant__ CUtensorMap tm_ys, const float *__restrict__ X, const float *__restrict__ cen, const float *__restrict__ wsc,
@@ -238,6 +248,8 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kWAS; s++) mbar_init(&S.a_full[s], 4), mbar_init(&S.a_empty[s], 1);
     for (int s = 0; s < kWWS; s++) mbar_init(&S.w_full[s], 1), mbar_init(&S.w_empty[s], 1);
+    // a slot is released by the 4 producer and the 8 epilogue warps
+    for (int s = 0; s < kWCS; s++) mbar_init(&S.cv_full[s], 1), mbar_init(&S.cv_empty[s], 12);
     mbar_init(&S.acc_full, 1);
     for (int q = 0; q < 4; q++) mbar_init(&S.acc_empty[q], 4);
     mbar_init(&S.mma_done, 1);
@@ -254,24 +266,34 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
     if (elect_one()) {
       tma_prefetch_desc(&tm_wh);
       tma_prefetch_desc(&tm_wl);
-      uint32_t wi = 0;
+      uint32_t wi = 0, ci = 0;
       bool ok = true;
       for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x)
-        for (int j = 0; j < K && ok; j++)
+        for (int j = 0; j < K && ok; j++, ci++) {
+          const int cs = ci % kWCS;
+          if (!(ok = mbar_wait(&S.cv_empty[cs], ((ci / kWCS) & 1) ^ 1, err))) break;
+          mbar_expect_tx(&S.cv_full[cs], (uint32_t)Dp * 8);
+          bulk_load_1d(S.cvm[cs], cen + (size_t)j * Dp, (uint32_t)Dp * 4, &S.cv_full[cs]);
+          bulk_load_1d(S.cvb[cs], wb + (size_t)j * Dp, (uint32_t)Dp * 4, &S.cv_full[cs]);
           for (int c = nc - 1; c >= 0; c--) {
             const int s = wi % kWWS;
             if (!(ok = mbar_wait(&S.w_empty[s], ((wi / kWWS) & 1) ^ 1, err))) break;
             const int rows = Dp - 64 * c;   // the triangle's nonzero rows of chunk c
             mbar_expect_tx(&S.w_full[s], (uint32_t)rows * 256);
             for (int rb = 0; rb < rows / 64; rb++) {
-              tma_load_2d(S.wh[s] + rb * 64 * 64, &tm_wh, &S.w_full[s], 64 * c, j * Dp + 64 * rb);
-              tma_load_2d(S.wl[s] + rb * 64 * 64, &tm_wl, &S.w_full[s], 64 * c, j * Dp + 64 * rb);
+              tma_load_2d(w_stage(S.wh, s) + rb * 64 * 64, &tm_wh, &S.w_full[s], 64 * c, j * Dp + 64 * rb);
+              tma_load_2d(w_stage(S.wl, s) + rb * 64 * 64, &tm_wl, &S.w_full[s], 64 * c, j * Dp + 64 * rb);
             }
             wi++;
           }
+        }
       for (int s = 0; s < kWWS && wi > (uint32_t)s; s++) {
         const uint32_t u = wi - 1 - s;
         mbar_wait_drain(&S.w_full[u % kWWS], (u / kWWS) & 1);
+      }
+      for (int s = 0; s < kWCS && ci > (uint32_t)s; s++) {
+        const uint32_t u = ci - 1 - s;
+        mbar_wait_drain(&S.cv_full[u % kWCS], (u / kWCS) & 1);
       }
     }
   } else if (warp == 1) {
@@ -290,7 +312,8 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
             if (!(ok = mbar_wait(&S.w_full[sw], (wi / kWWS) & 1, err))) break;
             tc_fence_after();
             const uint64_t dah = sdesc_sw128(smem_u32(S.ah[sa])), dal = sdesc_sw128(smem_u32(S.al[sa]));
-            const uint64_t dwh = sdesc_sw128(smem_u32(S.wh[sw])), dwl = sdesc_sw128(smem_u32(S.wl[sw]));
+            const uint64_t dwh = sdesc_sw128(smem_u32(w_stage(S.wh, sw)));
+            const uint64_t dwl = sdesc_sw128(smem_u32(w_stage(S.wl, sw)));
 #pragma unroll
             for (int t = 3; t >= 0; t--) {
               // +32 bytes per 16-element k-step inside the 128-byte swizzle row
@@ -314,7 +337,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
     // ------------------------------------------------ producers: a = x - m -> FP16 hi / lo
     const int quad = warp & 3, row = quad * 32 + lane;
     const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
-    uint32_t ai = 0;
+    uint32_t ai = 0, ci = 0;
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       const int64_t pt = tile * kWTile + row;
@@ -342,46 +365,47 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
         }
       }
       tmem_wait_st();
-      for (int j = 0; j < K && ok; j++) {
-        const float *mj = cen + (size_t)j * Dp;
+      for (int j = 0; j < K && ok; j++, ci++) {
+        const int cs = ci % kWCS;
+        if (!(ok = mbar_wait_warp(&S.cv_full[cs], (ci / kWCS) & 1, err))) break;
+        const float *mj = S.cvm[cs];
         for (int c = nc - 1; c >= 0; c--) {
           const int sa = ai % kWAS;
           if (!(ok = mbar_wait_warp(&S.a_empty[sa], ((ai / kWAS) & 1) ^ 1, err))) break;
           uint8_t *dh = reinterpret_cast<uint8_t *>(S.ah[sa]) + row * 128;
           uint8_t *dl = reinterpret_cast<uint8_t *>(S.al[sa]) + row * 128;
+          uint32_t x[64];
+          tmem_ld64(tbase + lane_addr + kWXCol + 64 * c, x);
+          tmem_wait_ld();
+          const float *mc = mj + 64 * c;
 #pragma unroll
-          for (int pg = 0; pg < 2; pg++) {   // two 32-dim halves of the chunk
-            uint32_t x[32];
-            tmem_ld32(tbase + lane_addr + kWXCol + 64 * c + 32 * pg, x);
-            tmem_wait_ld();
-            const float *mc = mj + 64 * c + 32 * pg;
-  #pragma unroll
-            for (int qq = 0; qq < 4; qq++) {
-              const int q = 4 * pg + qq;    // 16-byte chunk of the 128-byte operand row
-              const float4 m0 = __ldg(reinterpret_cast<const float4 *>(mc + 8 * qq));
-              const float4 m1 = __ldg(reinterpret_cast<const float4 *>(mc + 8 * qq + 4));
-              const float a[8] = {__uint_as_float(x[8 * qq]) - m0.x,     __uint_as_float(x[8 * qq + 1]) - m0.y,
-                                  __uint_as_float(x[8 * qq + 2]) - m0.z, __uint_as_float(x[8 * qq + 3]) - m0.w,
-                                  __uint_as_float(x[8 * qq + 4]) - m1.x, __uint_as_float(x[8 * qq + 5]) - m1.y,
-                                  __uint_as_float(x[8 * qq + 6]) - m1.z, __uint_as_float(x[8 * qq + 7]) - m1.w};
-              uint32_t hw[4], lw[4];
-  #pragma unroll
-              for (int u = 0; u < 4; u++) {
-                const __half2 hh = __floats2half2_rn(a[2 * u], a[2 * u + 1]);
-                const float2 f = __half22float2(hh);
-                hw[u] = h2_bits(hh);
-                lw[u] = h2_bits(__floats2half2_rn(a[2 * u] - f.x, a[2 * u + 1] - f.y));
-              }
-              const int off = (q ^ (row & 7)) << 4;   // 128-byte swizzle of 16-byte chunks
-              *reinterpret_cast<uint4 *>(dh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-              *reinterpret_cast<uint4 *>(dl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+          for (int q = 0; q < 8; q++) {       // 16-byte chunk of the 128-byte operand row
+            const float4 m0 = *reinterpret_cast<const float4 *>(mc + 8 * q);
+            const float4 m1 = *reinterpret_cast<const float4 *>(mc + 8 * q + 4);
+            const float a[8] = {__uint_as_float(x[8 * q]) - m0.x,     __uint_as_float(x[8 * q + 1]) - m0.y,
+                                __uint_as_float(x[8 * q + 2]) - m0.z, __uint_as_float(x[8 * q + 3]) - m0.w,
+                                __uint_as_float(x[8 * q + 4]) - m1.x, __uint_as_float(x[8 * q + 5]) - m1.y,
+                                __uint_as_float(x[8 * q + 6]) - m1.z, __uint_as_float(x[8 * q + 7]) - m1.w};
+            uint32_t hw[4], lw[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const __half2 hh = __floats2half2_rn(a[2 * u], a[2 * u + 1]);
+              const float2 f = __half22float2(hh);
+              hw[u] = h2_bits(hh);
+              lw[u] = h2_bits(__floats2half2_rn(a[2 * u] - f.x, a[2 * u + 1] - f.y));
             }
+            const int off = (q ^ (row & 7)) << 4;   // 128-byte swizzle of 16-byte chunks
+            *reinterpret_cast<uint4 *>(dh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+            *reinterpret_cast<uint4 *>(dl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
           }
           fence_async_shared();
           __syncwarp();
           if (lane == 0) mbar_arrive(&S.a_full[sa]);
           ai++;
         }
+        if (!ok) break;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.cv_empty[cs]);
       }
     }
   } else {
@@ -425,13 +449,15 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
       for (int j = 0; j < K; j++, ui++) {
         float lp = 0.f;
         if (eg == 0 && have_prev && prev_i >= 0) lp = scr[(size_t)(prev_par * K + j) * kWTile];
+        const int cs = ui % kWCS;
         ok = mbar_wait_warp(&S.acc_full, ui & 1, err);
+        if (ok) ok = mbar_wait_warp(&S.cv_full[cs], (ui / kWCS) & 1, err);
         // the group's warps take the same branch (its named barrier is inside)
         ok = bar_and(gbar, 128, ok);
         float s4[4] = {0.f, 0.f, 0.f, 0.f};
         if (ok) {
           tc_fence_after();
-          const float *bj = wb + (size_t)j * Dp;
+          const float *bj = S.cvb[cs];
           const float sc = wsc[j];
           for (int q = eg; q < nc; q += 2) {
             uint32_t v[64];
@@ -449,7 +475,7 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
 #pragma unroll
             for (int u = 0; u < 16; u++) {
               const int p0 = 64 * q + 4 * u;
-              const float4 b = __ldg(reinterpret_cast<const float4 *>(bj + p0));
+              const float4 b = *reinterpret_cast<const float4 *>(bj + p0);
               const float y[4] = {fmaf(__uint_as_float(v[4 * u]), sc, -b.x),
                                   fmaf(__uint_as_float(v[4 * u + 1]), sc, -b.y),
                                   fmaf(__uint_as_float(v[4 * u + 2]), sc, -b.z),
@@ -471,6 +497,8 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
               bulk_commit();
             }
           }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&S.cv_empty[cs]);
         }
         float s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
         if (eg == 1) S.ssum[ui & 1][row] = s;

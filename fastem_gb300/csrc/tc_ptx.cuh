@@ -16,6 +16,11 @@ namespace fem {
 namespace tc {
 
 constexpr long long kWaitBudgetCycles = 4000000000LL;  // ~2 s at 2 GHz
+// the status word (global memory) is read at most this often by a waiting
+// thread: an L2 round trip in every retry loop would delay the waiter's view
+// of an arrival by that much, and another role's failure only needs to be
+// seen within microseconds
+constexpr long long kErrPollCycles = 65536;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -72,21 +77,26 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parit
   return ok != 0;
 }
 
-// bounded wait for the phase with the given parity to complete; the error
-// flag and the clock budget are checked every 64 tries
+// bounded wait for the phase with the given parity to complete; the clock
+// budget is checked every 64 tries, the error flag every kErrPollCycles
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err,
                                           long long budget = kWaitBudgetCycles) {
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
+  long long poll = t0 + kErrPollCycles;
   while (true) {
 #pragma unroll 1
     for (int i = 0; i < 64; i++)
       if (mbar_try_wait(a, parity)) return true;
-    if (*(volatile int *)err) return false;
-    if (clock64() - t0 > budget) {
+    const long long now = clock64();
+    if (now - t0 > budget) {
       atomicExch(err, 1);
       return false;
+    }
+    if (now > poll) {
+      if (*(volatile int *)err) return false;
+      poll = now + kErrPollCycles;
     }
   }
 }
@@ -111,13 +121,18 @@ __device__ __forceinline__ bool mbar_wait_lazy(uint64_t *bar, uint32_t parity, i
   const uint32_t a = smem_u32(bar);
   if (mbar_try_wait(a, parity)) return true;
   const long long t0 = clock64();
+  long long poll = t0 + kErrPollCycles;
   while (true) {
     __nanosleep(ns);
     if (mbar_try_wait(a, parity)) return true;
-    if (*(volatile int *)err) return false;
-    if (clock64() - t0 > budget) {
+    const long long now = clock64();
+    if (now - t0 > budget) {
       atomicExch(err, 1);
       return false;
+    }
+    if (now > poll) {
+      if (*(volatile int *)err) return false;
+      poll = now + kErrPollCycles;
     }
   }
 }
@@ -142,13 +157,13 @@ __device__ __forceinline__ bool mbar_wait_drain(uint64_t *bar, uint32_t parity,
   return true;
 }
 
-// named barrier `id` over `count` threads that also ANDs a predicate: every
-// participant gets the same answer
 // named barrier `id` over `count` threads (a multiple of 32)
 __device__ __forceinline__ void named_bar_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
+// named barrier `id` over `count` threads that also ANDs a predicate: every
+// participant gets the same answer
 __device__ __forceinline__ bool bar_and(int id, int count, bool v) {
   uint32_t r;
   asm volatile(
@@ -168,6 +183,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
       " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
       : "memory");
+}
+
+// global -> shared contiguous copy of `bytes` (a multiple of 16; both
+// addresses 16-byte aligned), completing on `bar` (complete_tx)
+__device__ __forceinline__ void bulk_load_1d(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
 }
 
 // shared -> global tile store (bulk async-group completion).  Elements outside
