@@ -545,6 +545,29 @@ k_wide_estep(const __grid_constant__ CUtensorMap tm_wh, const __grid_constant__ 
 }
 
 // ============================================================== M-step sums
+// One warp's share of a window flush: the 32-column groups g = t, t + 3, ...
+// of the FP32 window (TMEM lanes of the warp's quarter) added to the FP64
+// partials (or stored, for a slot's first window).  The three warps of a
+// lane quarter (two producer warps and one flush warp) take t = 0, 1, 2.
+__device__ __forceinline__ void wide_flush_share(uint32_t taddr, double *cp, int ncols, int t, bool first) {
+  for (int g = t; g < ncols / 32; g += 3) {
+    const int c0 = 32 * g;
+    uint32_t v[32];
+    tmem_ld32(taddr + c0, v);
+    tmem_wait_ld();
+    if (first) {
+#pragma unroll
+      for (int e = 0; e < 32; e++) cp[(size_t)(c0 + e) * 128] = (double)__uint_as_float(v[e]);
+    } else {
+      double o[32];
+#pragma unroll
+      for (int e = 0; e < 32; e++) o[e] = cp[(size_t)(c0 + e) * 128];
+#pragma unroll
+      for (int e = 0; e < 32; e++) cp[(size_t)(c0 + e) * 128] = o[e] + (double)__uint_as_float(v[e]);
+    }
+  }
+}
+
 // CTA c owns blocks [c T / G, (c + 1) T / G) of the component-major
 // (component, 64-point block) space, T = K nbk; slot = component - first
 // component of the range.
@@ -569,7 +592,7 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
   if (threadIdx.x == 0) {
     for (int s = 0; s < kVS; s++) mbar_init(&S.in_full[s], 1), mbar_init(&S.z_full[s], 8), mbar_init(&S.in_empty[s], 1);
     mbar_init(&S.acc_full, 1);
-    mbar_init(&S.acc_empty, 4);
+    mbar_init(&S.acc_empty, 12);   // the 8 producer and 4 flush warps
     mbar_init(&S.mma_done, 1);
     fence_mbar_init();
   }
@@ -639,13 +662,22 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
   } else if (warp < kWCFlush0) {
     // ------------------------------------------------ producers: z = fp16(sqrt r) y in place
     const int p = threadIdx.x - 64;   // row p
-    uint32_t i = 0;
-    bool ok = true;
-    // sum r, sum r y and sum z^2 (the diagonal: its increments are all positive,
-    // which the tensor core's truncating accumulation would bias low) of row p
-    // over the segment
+    const int pw = warp - 2;          // producer warp 0..7
+    const int quad = warp & 3;
+    const uint32_t lane_addr = (uint32_t)(quad * 32) << 16;
+    uint32_t i = 0, wnd = 0;
+    bool ok = true, first = true;
+    // block f's index within its component and position within its FP32
+    // window, kept as counters (a 64-bit division per block would sit on the
+    // producers' critical path)
+    int64_t fb = f0 % nbk;
+    int wpos = 0, slot = 0;           // slot = component of f - first component of the range
+    // sum r, sum r y and sum z^2 (the diagonal: its increments are all
+    // positive, which the tensor core's truncating accumulation would bias
+    // low) of row p over the segment
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
     for (int64_t f = f0; f < f1 && ok; f++, i++) {
+      if (f != f0 && fb == 0) first = true, wpos = 0, slot++;
       const int s = i % kVS;
       ok = mbar_wait_warp(&S.in_full[s], (i / kVS) & 1, err);
       if (ok && p < kVBlk) {
@@ -653,7 +685,9 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
         S.sr[s][p] = __float2half_rn(sqrtf(r));
         s0 += (double)r;
       }
-      // every producer leaves together when one of them gave up
+      // every producer leaves together when one of them gave up (a common
+      // barrier also keeps the eight warps in step: without it they drift
+      // apart and the block waits for the last)
       if (!(ok = bar_and(1, 256, ok))) break;
       {
         const int rw = p;
@@ -686,12 +720,30 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       fence_async_shared();
       __syncwarp();
       if (lane == 0) mbar_arrive(&S.z_full[s]);
-      if (f == f1 - 1 || (f % nbk) == nbk - 1) {
-        double *sp = spart + ((size_t)blockIdx.x * nslot + ((int)(f / nbk) - j0)) * kSPart;
+      const bool send = f == f1 - 1 || fb == nbk - 1;
+      if (send) {
+        double *sp = spart + ((size_t)blockIdx.x * nslot + slot) * kSPart;
         sp[p] = s1;
         sp[kWMax + p] = s2;
         if (p < kVBlk) sp[2 * kWMax + p] = s0;
         s0 = 0.0, s1 = 0.0, s2 = 0.0;
+      }
+      // the window's flush is shared with the flush warps (the producers would
+      // otherwise idle while the single accumulator is read out)
+      const bool wend = send || wpos == kVWin - 1;
+      wpos = wend ? 0 : wpos + 1;
+      fb = fb == nbk - 1 ? 0 : fb + 1;
+      if (wend) {
+        if (!(ok = mbar_wait_warp(&S.acc_full, wnd & 1, err))) break;
+        tc_fence_after();
+        const int row = quad * 32 + lane;
+        double *cp = cpart + ((size_t)blockIdx.x * nslot + slot) * (size_t)ncols * 128 + row;
+        wide_flush_share(tbase + lane_addr, cp, ncols, pw < 4 ? 0 : 1, first);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&S.acc_empty);
+        wnd++;
+        first = false;
       }
     }
   } else {
@@ -708,21 +760,7 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       if (!(ok = mbar_wait_warp(&S.acc_full, wnd & 1, err))) break;
       tc_fence_after();
       double *cp = cpart + ((size_t)blockIdx.x * nslot + ((int)(f / nbk) - j0)) * (size_t)ncols * 128 + row;
-      for (int c0 = 0; c0 < ncols; c0 += 32) {
-        uint32_t v[32];
-        tmem_ld32(tbase + lane_addr + c0, v);
-        tmem_wait_ld();
-        if (first) {
-#pragma unroll
-          for (int e = 0; e < 32; e++) cp[(size_t)(c0 + e) * 128] = (double)__uint_as_float(v[e]);
-        } else {
-          double o[32];
-#pragma unroll
-          for (int e = 0; e < 32; e++) o[e] = cp[(size_t)(c0 + e) * 128];
-#pragma unroll
-          for (int e = 0; e < 32; e++) cp[(size_t)(c0 + e) * 128] = o[e] + (double)__uint_as_float(v[e]);
-        }
-      }
+      wide_flush_share(tbase + lane_addr, cp, ncols, 2, first);
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&S.acc_empty);
