@@ -277,12 +277,16 @@ int orc_em_estep(int d, int64_t n, int k, const float *X, const double *pi,
   return ORC_OK;
 }
 
-int orc_em_mstep(int d, int64_t n, int k, const float *X, const double *post,
-                 double *pi, double *mu, double *sigma, int nthreads) {
-  nthreads = resolve_threads(nthreads);
-  const size_t kd = (size_t)k * d, kdd = (size_t)k * d * d;
+/* PosteriorSum and MeanSums per thread, reduced into thread 0's in thread
+ * order, mu = MeanSums / PosteriorSum: the same in SimpleMatrixEM::doMStep
+ * (EM2/MatrixEM.cpp:319-343) and CachedEM::ComputeMeansPostSum
+ * (EM2/CachedEM.cpp:88-118).  ps receives the posterior sums. */
+static void mstep_means(int d, int64_t n, int k, const float *X, const double *post, double *mu,
+                        std::vector<double> &ps, int nthreads) {
+  const size_t kd = (size_t)k * d;
   /* Step1ReducerData per thread: PosteriorSum[K], MeanSums[K x d] */
-  std::vector<double> ps((size_t)nthreads * k, 0.0), ms((size_t)nthreads * kd, 0.0);
+  ps.assign((size_t)nthreads * k, 0.0);
+  std::vector<double> ms((size_t)nthreads * kd, 0.0);
 #pragma omp parallel num_threads(nthreads)
   {
     int tid = omp_get_thread_num();
@@ -308,6 +312,60 @@ int orc_em_mstep(int d, int64_t n, int k, const float *X, const double *post,
   }
   for (int j = 0; j < k; j++)
     for (int q = 0; q < d; q++) mu[(size_t)j * d + q] = ms[(size_t)j * d + q] / ps[j];
+}
+
+int orc_em_mstep_cached(int d, int64_t n, int k, const float *X, const double *post,
+                        double *pi, double *mu, double *sigma, int nthreads) {
+  nthreads = resolve_threads(nthreads);
+  const size_t kdd = (size_t)k * d * d;
+  std::vector<double> ps;
+  mstep_means(d, n, k, X, post, mu, ps, nthreads);
+  /* CachedEM::ComputeCovariances (EM2/CachedEM.cpp:120-163): per thread and
+   * component, syr-style rank-1 updates of the upper triangle weighted by the
+   * unscaled posterior around the new means; after the reduction the sums
+   * are divided by the posterior sum (selfadjointView<Upper>). */
+  std::vector<double> cs((size_t)nthreads * kdd, 0.0);
+#pragma omp parallel num_threads(nthreads)
+  {
+    int tid = omp_get_thread_num();
+    int64_t off, cnt;
+    find_items(n, nthreads, tid, off, cnt);
+    std::vector<double> t(d);
+    for (int j = 0; j < k; j++) {
+      double *C = &cs[(size_t)tid * kdd + (size_t)j * d * d];
+      const double *mj = mu + (size_t)j * d;
+      for (int64_t i = off; i < off + cnt; i++) {
+        const double w = post[i * k + j];
+        const float *x = X + i * d;
+        for (int q = 0; q < d; q++) t[q] = (double)x[q] - mj[q];
+        for (int a = 0; a < d; a++) {
+          const double ta = w * t[a];
+          double *Ca = C + (size_t)a * d;
+          for (int b = a; b < d; b++) Ca[b] += ta * t[b];
+        }
+      }
+    }
+  }
+  for (int t = 1; t < nthreads; t++)
+    for (size_t q = 0; q < kdd; q++) cs[q] += cs[(size_t)t * kdd + q];
+  for (int j = 0; j < k; j++) {
+    const double *C = &cs[(size_t)j * d * d];
+    double *S = sigma + (size_t)j * d * d;
+    const double inv = 1.0 / ps[j];
+    for (int a = 0; a < d; a++)
+      for (int b = 0; b < d; b++) S[a * d + b] = inv * ((b >= a) ? C[a * d + b] : C[b * d + a]);
+    /* CachedEM::MStep (EM2/CachedEM.cpp:166-170): Probs /= TotalRowCount */
+    pi[j] = ps[j] / (double)n;
+  }
+  return ORC_OK;
+}
+
+int orc_em_mstep(int d, int64_t n, int k, const float *X, const double *post,
+                 double *pi, double *mu, double *sigma, int nthreads) {
+  nthreads = resolve_threads(nthreads);
+  const size_t kdd = (size_t)k * d * d;
+  std::vector<double> ps;
+  mstep_means(d, n, k, X, post, mu, ps, nthreads);
 
   /* Step2ReducerData per thread: CovSums[K][d x d] (upper filled) */
   std::vector<double> cs((size_t)nthreads * kdd, 0.0);
@@ -352,6 +410,15 @@ int orc_em_train(int d, int64_t n, int k, const float *X, double *pi,
                  double abort_thr, double reg_coef, int svd,
                  double *logl_trace, double *e_trace, int *iter_counter,
                  double *final_logl, int nthreads) {
+  return orc_em_train_order(d, n, k, X, pi, mu, sigma, max_sweeps, eps, abort_thr, reg_coef, svd, logl_trace,
+                            e_trace, iter_counter, final_logl, nthreads, 0);
+}
+
+int orc_em_train_order(int d, int64_t n, int k, const float *X, double *pi,
+                       double *mu, double *sigma, int max_sweeps, double eps,
+                       double abort_thr, double reg_coef, int svd,
+                       double *logl_trace, double *e_trace, int *iter_counter,
+                       double *final_logl, int nthreads, int cached) {
   std::vector<double> U((size_t)k * d * d), logdet(k), post((size_t)n * k);
   double prev = -std::numeric_limits<double>::max(), logl = prev;
   int failed;
@@ -369,7 +436,10 @@ int orc_em_train(int d, int64_t n, int k, const float *X, double *pi,
   int it;
   for (it = 1; it <= max_sweeps; it++) {
     orc_em_estep(d, n, k, X, pi, mu, U.data(), logdet.data(), post.data(), &logl, nthreads);
-    orc_em_mstep(d, n, k, X, post.data(), pi, mu, sigma, nthreads);
+    if (cached)
+      orc_em_mstep_cached(d, n, k, X, post.data(), pi, mu, sigma, nthreads);
+    else
+      orc_em_mstep(d, n, k, X, post.data(), pi, mu, sigma, nthreads);
     orc_em_regularize(d, k, reg_coef, sigma);
     st = orc_em_init_densities(d, k, sigma, U.data(), logdet.data(), &failed);
     if (st != ORC_OK) {

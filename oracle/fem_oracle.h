@@ -65,6 +65,13 @@ int orc_em_estep(int d, int64_t n, int k, const float *X, const double *pi,
 int orc_em_mstep(int d, int64_t n, int k, const float *X, const double *post,
                  double *pi, double *mu, double *sigma, int nthreads);
 
+/* CachedEM::MStep (EM2/CachedEM.cpp:88-170): the same means and posterior
+ * sums, covariances as rank-1 updates weighted by the unscaled posteriors
+ * around the new means, divided by the posterior sum after the reduction
+ * (SimpleMatrixEM scales every point by sqrt(r / N_j) first). */
+int orc_em_mstep_cached(int d, int64_t n, int k, const float *X, const double *post,
+                        double *pi, double *mu, double *sigma, int nthreads);
+
 /* EMAlgorithm::TrainNoCopy (EM2/EMAlgorithm.cpp:139-191) driving
  * SimpleMatrixEM.  pi/mu/sigma hold the initial mixture on entry and the
  * final one on return.  logl_trace/e_trace receive one value per sweep
@@ -76,6 +83,14 @@ int orc_em_train(int d, int64_t n, int k, const float *X, double *pi,
                  double abort_thr, double reg_coef, int svd,
                  double *logl_trace, double *e_trace, int *iter_counter,
                  double *final_logl, int nthreads);
+
+/* orc_em_train with the M-step order chosen: cached = 0 SimpleMatrixEM
+ * (orc_em_mstep), 1 CachedEM (orc_em_mstep_cached). */
+int orc_em_train_order(int d, int64_t n, int k, const float *X, double *pi,
+                       double *mu, double *sigma, int max_sweeps, double eps,
+                       double abort_thr, double reg_coef, int svd,
+                       double *logl_trace, double *e_trace, int *iter_counter,
+                       double *final_logl, int nthreads, int cached);
 
 /* ---- k-means ----------------------------------------------------------- */
 

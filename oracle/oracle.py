@@ -60,8 +60,11 @@ def lib():
         L.orc_cond_number.restype = f64
         L.orc_em_estep.argtypes = [i32, i64, i32, P, P, P, P, P, P, P, i32]
         L.orc_em_mstep.argtypes = [i32, i64, i32, P, P, P, P, P, i32]
+        L.orc_em_mstep_cached.argtypes = [i32, i64, i32, P, P, P, P, P, i32]
         L.orc_em_train.argtypes = [i32, i64, i32, P, P, P, P, i32, f64, f64, f64,
                                    i32, P, P, P, P, i32]
+        L.orc_em_train_order.argtypes = [i32, i64, i32, P, P, P, P, i32, f64, f64, f64,
+                                         i32, P, P, P, P, i32, i32]
         L.orc_km_iterate.argtypes = [i32, i64, i32, P, P, P, P, i32, i32]
         L.orc_km_iterate.restype = f64
         L.orc_km_run.argtypes = [i32, i64, i32, P, P, f64, i32, P, i32]
@@ -137,10 +140,22 @@ def mstep(X, post, nthreads=0):
     return pi, mu, sigma
 
 
+def mstep_cached(X, post, nthreads=0):
+    """CachedEM::MStep order (orc_em_mstep_cached)."""
+    X = _f32(X)
+    n, d = X.shape
+    post = np.ascontiguousarray(post, dtype=np.float64)
+    k = post.shape[1]
+    pi, mu, sigma = np.zeros(k), np.zeros((k, d)), np.zeros((k, d, d))
+    lib().orc_em_mstep_cached(d, n, k, _p(X), _p(post), _p(pi), _p(mu), _p(sigma), nthreads)
+    return pi, mu, sigma
+
+
 def em_train(X, pi, mu, sigma, max_sweeps, eps=1e-5, abort_thr=1e5, reg_coef=0.0,
-             svd=False, nthreads=0):
-    """EMAlgorithm::TrainNoCopy over SimpleMatrixEM.  Returns a dict with the
-    final mixture, the per-sweep LogL / e traces, IterCounter and status."""
+             svd=False, nthreads=0, cached=False):
+    """EMAlgorithm::TrainNoCopy over SimpleMatrixEM (cached=True: CachedEM's
+    M-step order).  Returns a dict with the final mixture, the per-sweep LogL /
+    e traces, IterCounter and status."""
     X = _f32(X)
     n, d = X.shape
     pi = np.array(pi, dtype=np.float64, copy=True)
@@ -151,9 +166,10 @@ def em_train(X, pi, mu, sigma, max_sweeps, eps=1e-5, abort_thr=1e5, reg_coef=0.0
     ee = np.full(max_sweeps, np.nan)
     it = ctypes.c_int(0)
     fl = ctypes.c_double(np.nan)
-    st = lib().orc_em_train(d, n, k, _p(X), _p(pi), _p(mu), _p(sigma), int(max_sweeps),
-                            float(eps), float(abort_thr), float(reg_coef), int(bool(svd)),
-                            _p(ll), _p(ee), ctypes.byref(it), ctypes.byref(fl), nthreads)
+    st = lib().orc_em_train_order(d, n, k, _p(X), _p(pi), _p(mu), _p(sigma), int(max_sweeps),
+                                  float(eps), float(abort_thr), float(reg_coef), int(bool(svd)),
+                                  _p(ll), _p(ee), ctypes.byref(it), ctypes.byref(fl), nthreads,
+                                  int(bool(cached)))
     sweeps = max(0, min(it.value - 1, max_sweeps))
     return dict(status=st, pi=pi, mu=mu, sigma=sigma, logl=ll[:sweeps], e=ee[:sweeps],
                 iter_counter=it.value, final_logl=fl.value)

@@ -159,6 +159,38 @@ def test_em_vs_numpy(oracle):
     np.testing.assert_allclose(r["sigma"], sg, rtol=1e-9, atol=1e-11)
 
 
+def test_cachedem_order_matches_simple_matrix_em(oracle):
+    """CachedEM (EM2/CachedEM.cpp:120-170) sums rank-1 updates weighted by the
+    unscaled posteriors and divides by the posterior sum after the reduction;
+    SimpleMatrixEM (EM2/MatrixEM.cpp:53-67,90-99) scales every point by
+    sqrt(r / N_j) first.  The library runs the second order for both
+    algorithms; the two differ by rounding only: the same IterCounter and
+    LogL traces within 1e-12 per point, here and with the Eps rule."""
+    X, _ = synth.em_small(seed=11, n=8000, d=8, k=5)
+    oracle.rng_seed(3)
+    pi0, mu0, s0 = synth.identity_init(oracle.kmeans_plusplus(X, 5))
+    a = oracle.em_train(X, pi0, mu0, s0, 25, eps=0.0, nthreads=3)
+    b = oracle.em_train(X, pi0, mu0, s0, 25, eps=0.0, nthreads=3, cached=True)
+    assert a["status"] == b["status"] == 0 and a["iter_counter"] == b["iter_counter"]
+    assert np.max(np.abs(a["logl"] - b["logl"])) / len(X) < 1e-12
+    np.testing.assert_allclose(b["mu"], a["mu"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(b["sigma"], a["sigma"], rtol=1e-9, atol=1e-12)
+    # one M-step from the same posteriors: rounding-level differences only
+    st, U, logdet, _ = oracle.init_densities(s0)
+    assert st == 0
+    post, _ = oracle.estep(X, pi0, mu0, U, logdet)
+    ps, ms, ss = oracle.mstep(X, post)
+    pc, mc, sc = oracle.mstep_cached(X, post)
+    np.testing.assert_array_equal(pc, ps)
+    np.testing.assert_array_equal(mc, ms)
+    np.testing.assert_allclose(sc, ss, rtol=1e-12, atol=1e-14)
+    # with the convergence rule the sweep counts agree too
+    c = oracle.em_train(X, pi0, mu0, s0, 500, eps=1e-7, nthreads=2)
+    e = oracle.em_train(X, pi0, mu0, s0, 500, eps=1e-7, nthreads=2, cached=True)
+    assert c["iter_counter"] == e["iter_counter"]
+    np.testing.assert_allclose(e["final_logl"], c["final_logl"], rtol=1e-12)
+
+
 def test_em_thread_count_independent(oracle):
     X, _ = synth.em_small(seed=8, n=5000, d=4, k=3)
     pi0, mu0, s0 = synth.forgy_init(X, 3, seed=1)
