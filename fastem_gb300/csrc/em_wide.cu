@@ -734,7 +734,11 @@ k_wide_cov(const __grid_constant__ CUtensorMap tm_y, const __grid_constant__ CUt
       wpos = wend ? 0 : wpos + 1;
       fb = fb == nbk - 1 ? 0 : fb + 1;
       if (wend) {
-        if (!(ok = mbar_wait_warp(&S.acc_full, wnd & 1, err))) break;
+        // every producer reaches this point on the same block; they leave
+        // together (the per-block barrier above would otherwise wait for a
+        // warp that gave up here)
+        ok = mbar_wait_warp(&S.acc_full, wnd & 1, err);
+        if (!(ok = bar_and(1, 256, ok))) break;
         tc_fence_after();
         const int row = quad * 32 + lane;
         double *cp = cpart + ((size_t)blockIdx.x * nslot + slot) * (size_t)ncols * 128 + row;
